@@ -1,0 +1,339 @@
+"""Benchmark: batched rigid-body step, instance-steps/s on one GB300.
+
+Workload (default): 65,536 serial revolute chains, n ~ U{2..48}, random
+principal axes, l ~ U(0.2, 1) m, m ~ U(0.5, 2) kg, rod inertias,
+q0 ~ U(−π, π), v0 ~ N(0, 1), open-loop τ ~ N(0, 1) resampled every 10 steps,
+semi-implicit Euler at dt = 5e-4.  One bench "step" is one integrator step of
+every instance; the timed region runs `--steps` of them in one persistent
+launch.  The line reports the mixed-precision throughput as `value`, the plain
+FP64 form beside it, and the per-step q̈ error of mixed against FP64.
+
+`--impl reference` times the CPU restatement of the reference's `simulate`
+(the Rust crate cannot be built here) on all host cores over a bounded sample
+of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "gorilla-physics_gb300"))
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "instance-steps/sec mixed vs FP64 GPU at stated qdd error"
+UNIT = "instance-steps/s"
+DT = {0: 1e-3, 1: 5e-4, 2: 1e-4, 3: 2e-4}
+CONFIG_NAME = {0: "acrobot", 1: "serial-chain", 2: "floating-cube", 3: "quadruped"}
+CONTROL = {0: "host", 1: "open_loop", 2: "host", 3: "pd"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpb", choices=["gpb", "reference"])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--instances", type=int, default=65536)
+    ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
+    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"])
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, val in zip(names, f[5:9]):
+                    if val.lower().startswith("active"):
+                        reasons.add(n)
+        finally:
+            os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference(model, q0, v0, aux, config, steps, seconds_target=12.0, threads=None):
+    """The oracle (CPU restatement of the reference path) on a bounded sample."""
+    import oracle
+
+    threads = threads or os.cpu_count() or 1
+    qo, vo, _ = model.offsets()
+    sample = min(model.n, 4096)
+    K = max(1, steps)
+    # calibrate on a tiny run, then size the sample to ≈ seconds_target
+    cal_n = min(sample, 8 * threads)
+    q, v = q0.copy(), v0.copy()
+    kw = dict(control=CONTROL[config], ctl_all=aux if config == 3 else None, seed=7,
+              resample_every=10, sigma=1.0, kp=50.0, kd=2.0, threads=threads)
+    t = time.perf_counter()
+    oracle.simulate_batch(model, q, v, DT[config], 2, end=cal_n, **kw)
+    per = (time.perf_counter() - t) / (cal_n * 2)
+    K = max(1, min(K, int(seconds_target / max(per * sample, 1e-9))))
+    if K < 5:
+        sample = max(threads, int(seconds_target / max(per * 5, 1e-9)))
+        sample = min(sample, model.n)
+        K = 5
+    q, v = q0.copy(), v0.copy()
+    t = time.perf_counter()
+    oracle.simulate_batch(model, q, v, DT[config], K, end=sample, **kw)
+    dt = time.perf_counter() - t
+    return {"value": sample * K / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {sample} of {model.n} instances x {K} steps "
+                      f"(oracle restatement, {threads} host threads)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from gpb import Model
+
+    M, q0, v0, aux = Model.from_config(args.config, args.instances, seed=args.seed)
+    import oracle
+
+    oracle.build()
+    threads = os.cpu_count() or 1
+    qo, vo, _ = M.offsets()
+    sample = min(M.n, 4096)
+    kw = dict(control=CONTROL[args.config], ctl_all=aux if args.config == 3 else None, seed=7,
+              resample_every=10, sigma=1.0, kp=50.0, kd=2.0, threads=threads)
+    q, v = q0.copy(), v0.copy()
+    # per step: one integrator step of the sampled instances; sized so that the
+    # whole --steps run stays within a few minutes
+    t = time.perf_counter()
+    oracle.simulate_batch(M, q, v, DT[args.config], 1, end=min(sample, 64 * threads), **kw)
+    per_inst_step = (time.perf_counter() - t) / min(sample, 64 * threads)
+    budget = 120.0
+    sample = int(min(sample, max(threads, budget / max(args.steps * per_inst_step, 1e-9))))
+    for _ in range(args.warmup):
+        oracle.simulate_batch(M, q, v, DT[args.config], 1, end=sample, **kw)
+    t = time.perf_counter()
+    oracle.simulate_batch(M, q, v, DT[args.config], args.steps, end=sample, **kw)
+    el = time.perf_counter() - t
+    value = sample * args.steps / el
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
+        "impl": "reference",
+        "config": {"workload": f"{CONFIG_NAME[args.config]} x {args.instances}",
+                   "instances_timed": sample, "dt": DT[args.config], "integrator": "semi-implicit Euler"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"first {sample} instances x {args.steps} steps, oracle "
+                                   f"restatement of the reference path (Rust crate unbuildable here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def qdd_error(B, gpb):
+    a = B.dynamics_continuous(None, precision=gpb.FP64)
+    b = B.dynamics_continuous(None, precision=gpb.MIXED)
+    vo = B.v_offset
+    err = np.zeros(B.n)
+    for i in range(B.n):
+        x, y = b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]
+        err[i] = np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1.0)
+    return {"max": float(err.max()), "p99": float(np.quantile(err, 0.99)),
+            "median": float(np.median(err)), "norm": "‖Δq̈‖∞ / max(‖q̈_fp64‖∞, 1)"}
+
+
+def run_gpu(args):
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import gpb
+    from gpb import Batch, Model
+    from gpb.flops import model_flops
+
+    L = gpb.lib()
+    ctx = gpb.Context(local)
+    # weak scaling: every rank owns its own instances (seed offset by rank)
+    M, q0, v0, aux = Model.from_config(args.config, args.instances, seed=args.seed + 1000 * rank)
+    B = Batch(M, ctx)
+    flops_step = float(model_flops(M, 0).sum())
+    kw = dict(control=CONTROL[args.config], tau=aux if args.config == 3 else None, seed=7,
+              resample_every=10, sigma=1.0, kp=50.0, kd=2.0)
+    dt = DT[args.config]
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def reduce_max(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    results = {}
+    precs = {"both": ["fp64", "mixed"], "mixed": ["mixed"], "fp64": ["fp64"]}[args.precision]
+    for name in precs:
+        prec = gpb.FP64 if name == "fp64" else gpb.MIXED
+        B.update(q0, v0)
+        B.clear_status()
+        if args.warmup:
+            B.simulate_steps(args.warmup, dt, 0, prec, step0=0, **kw)
+        barrier()
+        ctx.synchronize()
+        with Clocks(local) as clk:
+            l0 = ctx.launches
+            t0 = time.perf_counter()
+            B.simulate_steps(args.steps, dt, 0, prec, step0=args.warmup, **kw)
+            kernel_ms = L.gpb_last_launch_ms(ctx.h)
+            ctx.synchronize()
+            wall = time.perf_counter() - t0
+            timed_launches = ctx.launches - l0
+        barrier()
+        kernel_ms = reduce_max(kernel_ms)
+        bad = int(np.sum(B.status() != 0))
+        results[name] = {"kernel_ms": kernel_ms, "wall_s": wall, "clocks": clk.summary(),
+                         "failed_instances": bad, "launches": timed_launches}
+    # q̈ error of mixed against FP64 at the final state
+    err = qdd_error(B, gpb) if len(precs) == 2 else None
+    # e2e through the public API: host (pinned) state in, K steps, state out
+    q_h = torch.from_numpy(q0).pin_memory()
+    v_h = torch.from_numpy(v0).pin_memory()
+    qn, vn = q_h.numpy(), v_h.numpy()
+    prec = gpb.MIXED if "mixed" in precs else gpb.FP64
+    barrier()
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    B.update(qn, vn)
+    B.simulate_steps(args.steps, dt, 0, prec, step0=0, **kw)
+    qo, vo_ = B.state()
+    e2e_s = time.perf_counter() - t0
+    e2e_s = reduce_max(e2e_s)
+
+    n_all = args.instances * world
+    head = results["mixed" if "mixed" in results else "fp64"]
+    value = n_all * args.steps / (head["kernel_ms"] * 1e-3)
+
+    def peak(precision):
+        t = __import__("ctypes").c_double()
+        gpb._abi.check(L.gpb_fma_peak(local, precision, 32, __import__("ctypes").byref(t)), "gpb_fma_peak")
+        return t.value
+
+    p64, p32 = peak(gpb.FP64), peak(gpb.MIXED)
+
+    def roof(res, bound, pk):
+        ach = flops_step * args.steps / (res["kernel_ms"] * 1e-3) / 1e12
+        return {"bound": bound, "achieved": ach, "peak": pk, "unit": "TFLOP/s", "frac": ach / pk,
+                "traffic": None, "peak_source": "measured FMA microbenchmark (gpb_fma_peak), this run",
+                "work": f"{flops_step / args.instances:.0f} algorithmic flops per instance-step (mean)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["kernel_ms"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if "mixed" in results else "f64",
+        "data": "synthetic (seeded Philox4x32-10 draws of the configuration's distributions)",
+        "config": {"workload": f"{CONFIG_NAME[args.config]} x {args.instances} per GPU",
+                   "dof": "U{2..48}" if args.config == 1 else None, "dt": dt,
+                   "integrator": "semi-implicit Euler", "control": CONTROL[args.config],
+                   "l2": "inputs larger than L2 (topology + state + scratch > 129 MB)"},
+        "gpu_launches": head["launches"],
+    }
+    if "fp64" in results:
+        line["fp64"] = {"value": n_all * args.steps / (results["fp64"]["kernel_ms"] * 1e-3),
+                        "ms_per_step": results["fp64"]["kernel_ms"] / args.steps,
+                        "roofline": roof(results["fp64"], "fp64", p64)}
+    if "mixed" in results and "fp64" in results:
+        line["mixed_over_fp64"] = line["value"] / line["fp64"]["value"]
+        line["qdd_rel_err_mixed_vs_fp64"] = err
+    line["roofline"] = roof(head, "fp32" if "mixed" in results else "fp64",
+                            p32 if "mixed" in results else p64)
+    line["peaks_measured"] = {"fp64_tflops": p64, "fp32_tflops": p32}
+    line["clocks"] = head["clocks"]
+    line["failed_instances"] = {k: r["failed_instances"] for k, r in results.items()}
+    line["e2e"] = {"value": n_all * args.steps / e2e_s, "unit": UNIT,
+                   "h2d_bytes_per_step": (qn.nbytes + vn.nbytes) / args.steps,
+                   "d2h_bytes_per_step": (qo.nbytes + vo_.nbytes) / args.steps,
+                   "note": "gpb_set_state (pinned host) + gpb_simulate + gpb_get_state"}
+    if rank == 0 and not args.skip_cpu:
+        line["cpu_baseline"] = cpu_reference(M, q0, v0, aux, args.config, args.steps)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,129 @@
+// Internal structures shared by the host library (gpb_host.cpp) and the CUDA
+// kernels (gpb_kernels.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gpb {
+
+// Instances are stored in packs of LANES (one warp, one instance per lane).
+// Every per-instance array is "lane-interleaved": element e of the instance in
+// lane l of a pack lives at base_row(pack) * LANES + e * LANES + l, so that the
+// 32 lanes of a warp touch 32 consecutive words.
+constexpr int LANES = 32;
+
+// Topology word 0 of a body: joint type | parent << 4 | qo << 12 | vo << 22.
+// Word 1: flags (bits 0-7) | first contact << 8 | contact count << 16.
+enum BodyFlags : uint32_t {
+  BF_INIT_ROT_IDENTITY = 1u << 0,  // init rotation is the identity
+  BF_AXIS_PRINCIPAL = 1u << 1,     // axis is ±x, ±y or ±z (index in bits 2-3, sign bit 4)
+  BF_AXIS_NEG = 1u << 4,
+  BF_BRANCH = 1u << 5,             // some child is not the next body: keep X, V, A in scratch
+  BF_SPRING = 1u << 6,             // prismatic spring
+  BF_DIAG_INERTIA = 1u << 7,       // body-frame moment is diagonal
+};
+__host__ __device__ inline uint32_t bf_axis_index(uint32_t flags) { return (flags >> 2) & 3u; }
+
+// Doubles (and floats) of one body in the topology table.
+constexpr int TOPO_D = 27;  // Rinit (9, row-major), tinit (3), axis (3), inertia (10), spring (2)
+constexpr int TD_RINIT = 0, TD_TINIT = 9, TD_AXIS = 12, TD_INERTIA = 15, TD_SPRING = 25;
+constexpr int CTC_D = 6;    // location (3), k, radius, damping
+constexpr int HS_D = 8;     // point (3), normal (3), alpha, mu
+constexpr int LANE_I = 8;   // per-lane ints: instance, nb, nq, nv, nc, nh, contact model, pad
+
+struct PackDesc {
+  int32_t count, nb, nq, nv, nc, nh, chain, pad;
+  // bases in rows (one row = LANES elements)
+  int64_t topo;   // topology bodies (2 int words / TOPO_D reals per body)
+  int64_t ctc;    // contacts
+  int64_t hs;     // half-spaces
+  int64_t q, v;   // state (doubles)
+  int64_t lane;   // per-lane ints
+  int64_t scr;    // scratch, in rows of 8-byte words
+};
+
+// Scratch sub-array offsets (rows of 8-byte words; R-typed arrays use the same
+// row pitch so that the float and double kernels share one layout).
+struct ScratchLayout {
+  int32_t X, V, A, S, I, F, M, D, rhs, q0, v0, qs, vs, facc, tau, cf, total;
+};
+__host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, int nc) {
+  ScratchLayout s;
+  int o = 0;
+  s.X = o; o += 12 * nb;
+  s.V = o; o += 6 * nb;
+  s.A = o; o += 6 * nb;
+  s.S = o; o += 6 * nv;
+  s.I = o; o += 10 * nb;
+  s.F = o; o += 6 * nb;
+  s.M = o; o += nv * (nv + 1) / 2;
+  s.D = o; o += nv;
+  s.rhs = o; o += nv;
+  s.q0 = o; o += nq;
+  s.v0 = o; o += nv;
+  s.qs = o; o += nq;
+  s.vs = o; o += nv;
+  s.facc = o; o += nv;
+  s.tau = o; o += nv;
+  s.cf = o; o += 3 * nc;
+  s.total = o;
+  return s;
+}
+
+// Everything a kernel launch needs (device pointers).
+struct DeviceBatch {
+  int32_t npacks;
+  const PackDesc* packs;
+  const uint32_t* topoW;   // 2 words per body
+  const double* topoD;
+  const float* topoF;
+  const int32_t* ctcI;     // body (0-based) | original index << 8
+  const double* ctcD;
+  const float* ctcF;
+  const double* hsD;
+  const float* hsF;
+  const int32_t* laneI;
+  int32_t* status;         // one int per lane row slot
+  double* q;
+  double* v;
+  double* tau_in;          // host torques or PD targets (pack layout)
+  double* scratch;
+  const int64_t* qmap;     // pack slot -> flat user index (-1 = padding)
+  const int64_t* vmap;
+  const int64_t* cmap;     // contact slot (3 per contact) -> flat user index
+  int64_t nq_total, nv_total, nc_total;
+  int32_t* queue;          // persistent-kernel work counter
+};
+
+struct StepParams {
+  double dt;
+  int64_t K;
+  int64_t step0;
+  int32_t integrator;
+  int32_t precision;
+  int32_t control;
+  uint32_t seed;
+  int32_t resample;
+  double sigma, kp, kd;
+  int64_t record_every;
+  double* history;      // device, [K/record_every][nq_total + nv_total]
+  double* qdd_out;      // dynamics-only: user-order q̈ (device)
+  double* cforce_out;   // dynamics-only: user-order contact forces (device)
+  int32_t tau_mode;     // dynamics/step: 0 = zero torque, 1 = tau_in holds torques
+};
+
+// Launchers (gpb_kernels.cu).  All return a cudaError_t.
+cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes_per_instance,
+                            int num_sms, cudaStream_t s);
+cudaError_t launch_dynamics(const DeviceBatch& b, const StepParams& p, cudaStream_t s);
+cudaError_t launch_scatter(const int64_t* map, int64_t slots, const double* src, double* dst,
+                           cudaStream_t s);
+cudaError_t launch_gather(const int64_t* map, int64_t slots, const double* src, double* dst,
+                          cudaStream_t s);
+
+// Open-loop torque draw shared bit for bit by host and device.
+__host__ __device__ double open_loop_tau(uint32_t seed, int64_t inst, int64_t block, int32_t dof,
+                                         double sigma);
+
+}  // namespace gpb

@@ -1,0 +1,755 @@
+// CUDA kernels (sm_103a) of the batched rigid-body step.
+//
+// Mapping "lane per instance": one warp owns a pack of 32 instances, one lane
+// per instance, and runs the whole step (forward kinematics, twists, bias
+// accelerations, contact, Newton–Euler, inward sweep, CRBA fill, Cholesky,
+// solve, integrator) serially for its instance.  Every FP64 instruction is
+// therefore issued with 32 useful lanes and no redundant work — on GB300 the
+// FP64 pipe is the bound of the plain-FP64 form, so work efficiency is what
+// counts.  Packs are filled with instances of the same topology class (sorted
+// on the host) so lanes stay converged.  A persistent grid pulls packs from a
+// device work counter and runs all K steps of a pack before taking the next.
+//
+// Reference algorithm: gorilla-physics src/dynamics.rs:322-364 (one dynamics
+// evaluation), src/integrators.rs:25-39,177-319 (integrators),
+// src/simulate.rs:87-112 (the K-step loop).
+
+#include <math.h>
+#include <string.h>
+
+#include "gpb_device.cuh"
+#include "gpb_internal.h"
+#include "gpb_rng.h"
+
+namespace gpb {
+
+constexpr double GRAVITY = 9.81;  // src/lib.rs:39
+
+__host__ __device__ double open_loop_tau(uint32_t seed, int64_t inst, int64_t block, int32_t dof,
+                                         double sigma) {
+  return sigma * polar_normal((uint32_t)inst, seed, (uint32_t)block, (uint32_t)dof, RNG_TAG_TAU);
+}
+
+// ---------------------------------------------------------------------------
+// Lane-strided column accessor: element e of this lane's instance.
+
+template <typename T>
+struct Col {
+  T* p;
+  __device__ __forceinline__ T& operator[](int e) const { return p[(size_t)e * LANES]; }
+};
+template <typename T>
+__device__ __forceinline__ Col<T> col_at(T* base, int64_t row, int lane) {
+  return Col<T>{base + row * LANES + lane};
+}
+
+template <typename R>
+struct RealTopo;
+template <>
+struct RealTopo<double> {
+  __device__ static const double* topo(const DeviceBatch& b) { return b.topoD; }
+  __device__ static const double* ctc(const DeviceBatch& b) { return b.ctcD; }
+  __device__ static const double* hs(const DeviceBatch& b) { return b.hsD; }
+};
+template <>
+struct RealTopo<float> {
+  __device__ static const float* topo(const DeviceBatch& b) { return b.topoF; }
+  __device__ static const float* ctc(const DeviceBatch& b) { return b.ctcF; }
+  __device__ static const float* hs(const DeviceBatch& b) { return b.hsF; }
+};
+
+// Per-lane context for one dynamics evaluation.
+template <typename R>
+struct LaneCtx {
+  int lane, nb, nq, nv, nc, nh, model, chain;
+  const uint32_t* W;  // topology words (row base applied, lane applied)
+  const R* T;         // topology reals
+  const int32_t* CI;  // contact ints
+  const R* CD;        // contact reals
+  const R* HD;        // half-space reals
+  ScratchLayout L;
+  R* sR;              // scratch viewed as R (row pitch = LANES * 8 bytes)
+  double* sD;         // scratch viewed as double
+  __device__ __forceinline__ uint32_t w(int e) const { return W[(size_t)e * LANES]; }
+  __device__ __forceinline__ R t(int e) const { return T[(size_t)e * LANES]; }
+  // R-typed scratch element (e in rows of 8-byte words)
+  __device__ __forceinline__ R& r(int e) const {
+    return *reinterpret_cast<R*>(reinterpret_cast<char*>(sR) + (size_t)e * LANES * 8);
+  }
+  __device__ __forceinline__ double& d(int e) const { return sD[(size_t)e * LANES]; }
+};
+
+template <typename R>
+__device__ __forceinline__ void store_sv(const LaneCtx<R>& c, int base, const SV<R>& s) {
+  c.r(base) = s.w.x;
+  c.r(base + 1) = s.w.y;
+  c.r(base + 2) = s.w.z;
+  c.r(base + 3) = s.v.x;
+  c.r(base + 4) = s.v.y;
+  c.r(base + 5) = s.v.z;
+}
+template <typename R>
+__device__ __forceinline__ SV<R> load_sv(const LaneCtx<R>& c, int base) {
+  return {{c.r(base), c.r(base + 1), c.r(base + 2)}, {c.r(base + 3), c.r(base + 4), c.r(base + 5)}};
+}
+template <typename R>
+__device__ __forceinline__ void store_si(const LaneCtx<R>& c, int base, const SI<R>& I) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) c.r(base + k) = I.j[k];
+  c.r(base + 6) = I.c.x;
+  c.r(base + 7) = I.c.y;
+  c.r(base + 8) = I.c.z;
+  c.r(base + 9) = I.m;
+}
+template <typename R>
+__device__ __forceinline__ SI<R> load_si(const LaneCtx<R>& c, int base) {
+  SI<R> I;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) I.j[k] = c.r(base + k);
+  I.c = {c.r(base + 6), c.r(base + 7), c.r(base + 8)};
+  I.m = c.r(base + 9);
+  return I;
+}
+
+// Rotation matrix of a unit quaternion (x, y, z, w).
+template <typename R>
+__device__ __forceinline__ M3<R> quat_to_mat(R x, R y, R z, R w) {
+  R xx = x * x, yy = y * y, zz = z * z, ww = w * w;
+  R xy = x * y * R(2), xz = x * z * R(2), yz = y * z * R(2);
+  R wx = w * x * R(2), wy = w * y * R(2), wz = w * z * R(2);
+  M3<R> m;
+  m.a[0] = ww + xx - yy - zz;
+  m.a[1] = xy - wz;
+  m.a[2] = xz + wy;
+  m.a[3] = xy + wz;
+  m.a[4] = ww - xx + yy - zz;
+  m.a[5] = yz - wx;
+  m.a[6] = xz - wy;
+  m.a[7] = yz + wx;
+  m.a[8] = ww - xx - yy + zz;
+  return m;
+}
+
+template <typename R>
+__device__ __forceinline__ void sincos_r(R a, R* s, R* c);
+template <>
+__device__ __forceinline__ void sincos_r<double>(double a, double* s, double* c) {
+  sincos(a, s, c);
+}
+template <>
+__device__ __forceinline__ void sincos_r<float>(float a, float* s, float* c) {
+  sincosf(a, s, c);
+}
+
+// Contact force of one point against one half-space (src/contact.rs:260-338),
+// or the linear spring–damper law.
+template <typename R>
+__device__ __forceinline__ V3<R> contact_force(int model, R z, V3<R> n, V3<R> vel, R k_point,
+                                               R damping, R alpha, R mu) {
+  R zdot = -dot(vel, n);
+  R pi;
+  if (model == 1) {
+    pi = fmax(k_point * z + damping * zdot, R(0));
+  } else {
+    // z^1.5 (NaN for z < 0 inside the margin → max(NaN, 0) = 0, like Rust)
+    R zn = z * sqrt(z);
+    R k = k_point * R(50e3) / (k_point + R(50e3));
+    R lam = R(1.5) * alpha * k;
+    pi = fmax(lam * zn * zdot + k * zn, R(0));
+  }
+  V3<R> f = n * pi;
+  V3<R> vt = vel + n * zdot;
+  R vtn = sqrt(dot(vt, vt));
+  if (vtn != R(0)) {
+    R s = vtn / R(1e-3);
+    R mue = s > R(1) ? mu : mu * s;
+    R g = -mue * pi / vtn;
+    f = f + vt * g;
+  }
+  return f;
+}
+
+// One dynamics evaluation (src/dynamics.rs:322-364): reads q, v, tau (double
+// columns), writes q̈ into `qdd`.  Returns GPB status bits.
+template <typename R, typename RC>
+__device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<double> tau,
+                             bool have_tau, Col<double> qdd, Col<double> cforce, bool want_cf) {
+  const R g = R(GRAVITY);
+  // ---- outward sweep --------------------------------------------------
+  M3<R> Rp;
+  V3<R> pp;
+  SV<R> Vp, Ap;
+  for (int b = 0; b < c.nb; ++b) {
+    uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
+    int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
+    uint32_t fl = w1 & 255;
+    // parent frame
+    M3<R> Rpar;
+    V3<R> ppar;
+    SV<R> Vpar, Apar;
+    if (parent == 0) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Rpar.a[k] = R(0);
+      Rpar.a[0] = Rpar.a[4] = Rpar.a[8] = R(1);
+      ppar = {R(0), R(0), R(0)};
+      Vpar = {{R(0), R(0), R(0)}, {R(0), R(0), R(0)}};
+      Apar = {{R(0), R(0), R(0)}, {R(0), R(0), g}};  // inverse gravity (src/dynamics.rs:211-218)
+    } else if (parent == b) {
+      Rpar = Rp;
+      ppar = pp;
+      Vpar = Vp;
+      Apar = Ap;
+    } else {
+      int pb = parent - 1;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Rpar.a[k] = c.r(c.L.X + 12 * pb + k);
+      ppar = {c.r(c.L.X + 12 * pb + 9), c.r(c.L.X + 12 * pb + 10), c.r(c.L.X + 12 * pb + 11)};
+      Vpar = load_sv(c, c.L.V + 6 * pb);
+      Apar = load_sv(c, c.L.A + 6 * pb);
+    }
+    const int tb = TOPO_D * b;
+    // A = Rpar · Rinit ;  p = ppar + Rpar · tinit
+    M3<R> Am;
+    if (fl & BF_INIT_ROT_IDENTITY) {
+      Am = Rpar;
+    } else {
+      M3<R> Ri;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Ri.a[k] = c.t(tb + TD_RINIT + k);
+      Am = mul(Rpar, Ri);
+    }
+    V3<R> ti{c.t(tb + TD_TINIT), c.t(tb + TD_TINIT + 1), c.t(tb + TD_TINIT + 2)};
+    V3<R> pb = ppar + mul(Rpar, ti);
+    M3<R> Rb;
+    SV<R> vj{{R(0), R(0), R(0)}, {R(0), R(0), R(0)}};  // S q̇ of this joint (world)
+    int nvb = 0;
+    SV<R> S[6];
+    if (type == 1 || type == 2) {  // revolute / prismatic
+      V3<R> ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
+      V3<R> aw = mul(Am, ax);  // world axis (R_b a = A a)
+      R qv = R(q[qo]);
+      if (type == 1) {
+        R s, co;
+        sincos_r<R>(qv, &s, &co);
+        if (fl & BF_AXIS_PRINCIPAL) {
+          int ai = bf_axis_index(fl);
+          R sg = (fl & BF_AXIS_NEG) ? -s : s;
+          int i1 = (ai + 1) % 3, i2 = (ai + 2) % 3;
+          Rb = Am;
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            R a1 = Am.a[3 * r + i1], a2 = Am.a[3 * r + i2];
+            Rb.a[3 * r + i1] = a1 * co + a2 * sg;
+            Rb.a[3 * r + i2] = a2 * co - a1 * sg;
+          }
+        } else {
+          // Rodrigues: Rot = c 1 + s [a]× + (1−c) a aᵀ ; Rb = A Rot
+          R omc = R(1) - co;
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            V3<R> ar{Am.a[3 * r], Am.a[3 * r + 1], Am.a[3 * r + 2]};
+            V3<R> x = cross(ar, ax);  // row · [a]× = (row × a)ᵀ... row_r [a]× = ar × a
+            R d = dot(ar, ax) * omc;
+            Rb.a[3 * r] = ar.x * co + x.x * s + ax.x * d;
+            Rb.a[3 * r + 1] = ar.y * co + x.y * s + ax.y * d;
+            Rb.a[3 * r + 2] = ar.z * co + x.z * s + ax.z * d;
+          }
+        }
+        S[0] = {aw, cross(pb, aw)};
+      } else {
+        Rb = Am;
+        pb = pb + aw * qv;
+        S[0] = {{R(0), R(0), R(0)}, aw};
+      }
+      nvb = 1;
+      vj = scale(S[0], R(v[vo]));
+    } else if (type == 3) {  // floating: pose (x,y,z,w,tx,ty,tz)
+      M3<R> Rq = quat_to_mat<R>(R(q[qo]), R(q[qo + 1]), R(q[qo + 2]), R(q[qo + 3]));
+      V3<R> tq{R(q[qo + 4]), R(q[qo + 5]), R(q[qo + 6])};
+      Rb = mul(Am, Rq);
+      pb = pb + mul(Am, tq);
+      nvb = 6;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        V3<R> ck = col(Rb, k);
+        S[k] = {ck, cross(pb, ck)};
+        S[3 + k] = {{R(0), R(0), R(0)}, ck};
+      }
+      V3<R> om{R(v[vo]), R(v[vo + 1]), R(v[vo + 2])};
+      V3<R> lv{R(v[vo + 3]), R(v[vo + 4]), R(v[vo + 5])};
+      V3<R> ow = mul(Rb, om);
+      vj = {ow, mul(Rb, lv) + cross(pb, ow)};
+    } else {  // fixed
+      Rb = Am;
+    }
+    SV<R> Vb = Vpar + vj;
+    SV<R> Ab = Apar + crm(Vb, vj);
+    for (int k = 0; k < nvb; ++k) store_sv(c, c.L.S + 6 * (vo + k), S[k]);
+    // world inertia and Newton–Euler (src/dynamics.rs:41-100)
+    SI<R> Ib;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) Ib.j[k] = c.t(tb + TD_INERTIA + 4 + k);
+    Ib.c = {c.t(tb + TD_INERTIA + 1), c.t(tb + TD_INERTIA + 2), c.t(tb + TD_INERTIA + 3)};
+    Ib.m = c.t(tb + TD_INERTIA);
+    // j order in the table: xx, yy, zz, xy, xz, yz
+    SI<R> Iw = to_world(Ib, Rb, pb, (fl & BF_DIAG_INERTIA) != 0);
+    SV<R> f = imul(Iw, Ab) + crf(Vb, imul(Iw, Vb));
+    // contacts of this body (src/contact.rs:97-128) → f −= W_contact
+    int cb = (w1 >> 8) & 255, cn = (w1 >> 16) & 255;
+    for (int k = cb; k < cb + cn; ++k) {
+      const int cd = CTC_D * k;
+      V3<R> loc{c.CD[(size_t)cd * LANES], c.CD[(size_t)(cd + 1) * LANES],
+                c.CD[(size_t)(cd + 2) * LANES]};
+      R kp = c.CD[(size_t)(cd + 3) * LANES], rad = c.CD[(size_t)(cd + 4) * LANES],
+        damp = c.CD[(size_t)(cd + 5) * LANES];
+      V3<R> pw = mul(Rb, loc) + pb;
+      V3<R> fsum{R(0), R(0), R(0)};
+      for (int h = 0; h < c.nh; ++h) {
+        const int hd = HS_D * h;
+        V3<R> hp{c.HD[(size_t)hd * LANES], c.HD[(size_t)(hd + 1) * LANES], c.HD[(size_t)(hd + 2) * LANES]};
+        V3<R> hn{c.HD[(size_t)(hd + 3) * LANES], c.HD[(size_t)(hd + 4) * LANES],
+                 c.HD[(size_t)(hd + 5) * LANES]};
+        R al = c.HD[(size_t)(hd + 6) * LANES], mu = c.HD[(size_t)(hd + 7) * LANES];
+        R dist = dot(pw - hp, hn);
+        V3<R> app = pw;
+        R pen;
+        if (rad > R(0)) {
+          if (!(dist - rad <= R(1e-8))) continue;
+          pen = rad - dist;
+          app = pw - hn * rad;
+        } else {
+          if (!(dist <= R(1e-8))) continue;  // HalfSpace::has_inside (margin 1e-8)
+          pen = -dist;
+        }
+        V3<R> vel = Vb.v + cross(Vb.w, app);
+        V3<R> fc = contact_force<R>(c.model, pen, hn, vel, kp, damp, al, mu);
+        f.w = f.w - cross(app, fc);
+        f.v = f.v - fc;
+        fsum = fsum + fc;
+      }
+      if (want_cf) {
+        int orig = (c.CI[(size_t)k * LANES] >> 8) & 255;
+        cforce[3 * orig] = double(fsum.x);
+        cforce[3 * orig + 1] = double(fsum.y);
+        cforce[3 * orig + 2] = double(fsum.z);
+      }
+    }
+    store_si(c, c.L.I + 10 * b, Iw);
+    store_sv(c, c.L.F + 6 * b, f);
+    if (fl & BF_BRANCH) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) c.r(c.L.X + 12 * b + k) = Rb.a[k];
+      c.r(c.L.X + 12 * b + 9) = pb.x;
+      c.r(c.L.X + 12 * b + 10) = pb.y;
+      c.r(c.L.X + 12 * b + 11) = pb.z;
+      store_sv(c, c.L.V + 6 * b, Vb);
+      store_sv(c, c.L.A + 6 * b, Ab);
+    }
+    Rp = Rb;
+    pp = pb;
+    Vp = Vb;
+    Ap = Ab;
+  }
+
+  // ---- inward sweep: composite inertia, joint forces, CRBA fill -------
+  const int nv = c.nv;
+  if (!c.chain) {
+    // Non-ancestor pairs are not written by the fill but hold Cholesky fill-in
+    // from the previous evaluation: clear the packed triangle first.
+    const int nm = nv * (nv + 1) / 2;
+    for (int e = 0; e < nm; ++e) c.d(c.L.M + e) = 0.0;
+  }
+  SI<R> cI;
+  SV<R> cF;
+  int ctarget = -1;
+  for (int b = c.nb - 1; b >= 0; --b) {
+    uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
+    int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
+    SI<R> Ic = load_si(c, c.L.I + 10 * b);
+    SV<R> f = load_sv(c, c.L.F + 6 * b);
+    if (ctarget == b) {
+      iadd(Ic, cI);
+      f = f + cF;
+    }
+    int nvb = type == 3 ? 6 : (type == 0 ? 0 : 1);
+    for (int k = 0; k < nvb; ++k) {
+      SV<R> Sk = load_sv(c, c.L.S + 6 * (vo + k));
+      double rhs = have_tau ? tau[vo + k] : 0.0;
+      if (type == 2 && (w1 & BF_SPRING)) {  // src/dynamics.rs:298-315
+        const int tb = TOPO_D * b;
+        double ks = double(c.t(tb + TD_SPRING)), ls = double(c.t(tb + TD_SPRING + 1));
+        rhs += -ks * (q[qo] - ls);
+      }
+      c.d(c.L.rhs + vo + k) = rhs - double(sdot(Sk, f));
+      SV<R> Fk = imul(Ic, Sk);
+      // row vo+k of H: F_kᵀ S_l for every column l of this joint and its ancestors
+      int row = vo + k;
+      int rowbase = c.L.M + row * (row + 1) / 2;
+      for (int l = 0; l <= k; ++l) {
+        SV<R> Sl = l == k ? Sk : load_sv(c, c.L.S + 6 * (vo + l));
+        c.d(rowbase + vo + l) = double(sdot(Fk, Sl));
+      }
+      int a = parent;
+      while (a != 0) {
+        uint32_t wa = c.w(2 * (a - 1));
+        int ta = wa & 15, voa = (wa >> 22) & 1023;
+        int nva = ta == 3 ? 6 : (ta == 0 ? 0 : 1);
+        for (int l = 0; l < nva; ++l) {
+          SV<R> Sl = load_sv(c, c.L.S + 6 * (voa + l));
+          c.d(rowbase + voa + l) = double(sdot(Fk, Sl));
+        }
+        a = (wa >> 4) & 255;
+      }
+    }
+    if (parent != 0) {
+      int pb = parent - 1;
+      if (pb == b - 1) {
+        cI = Ic;
+        cF = f;
+        ctarget = pb;
+      } else {
+        SI<R> Ip = load_si(c, c.L.I + 10 * pb);
+        iadd(Ip, Ic);
+        store_si(c, c.L.I + 10 * pb, Ip);
+        SV<R> fp = load_sv(c, c.L.F + 6 * pb) + f;
+        store_sv(c, c.L.F + 6 * pb, fp);
+        ctarget = -1;
+      }
+    } else {
+      ctarget = -1;
+    }
+  }
+
+  // ---- Cholesky (row by row) and the two triangular solves -------------
+  // M holds H in packed lower storage; entries of non-ancestor pairs were
+  // zeroed before the call (trees) or are all written (chains).
+  int st = 0;
+  for (int i = 0; i < nv; ++i) {
+    int ri = c.L.M + i * (i + 1) / 2;
+    for (int j = 0; j <= i; ++j) {
+      int rj = c.L.M + j * (j + 1) / 2;
+      RC s = RC(c.d(ri + j));
+      for (int k = 0; k < j; ++k) s -= RC(c.d(ri + k)) * RC(c.d(rj + k));
+      if (i == j) {
+        if (!(s > RC(0))) {
+          st |= 2;  // GPB_ST_CHOL_FAIL
+          s = RC(1);
+        }
+        RC l = sqrt(s);
+        c.d(ri + i) = double(l);
+        c.d(c.L.D + i) = double(RC(1) / l);
+      } else {
+        c.d(ri + j) = double(s * RC(c.d(c.L.D + j)));
+      }
+    }
+  }
+  for (int i = 0; i < nv; ++i) {
+    int ri = c.L.M + i * (i + 1) / 2;
+    RC s = RC(c.d(c.L.rhs + i));
+    for (int k = 0; k < i; ++k) s -= RC(c.d(ri + k)) * RC(c.d(c.L.rhs + k));
+    c.d(c.L.rhs + i) = double(s * RC(c.d(c.L.D + i)));
+  }
+  for (int i = nv - 1; i >= 0; --i) {
+    RC s = RC(c.d(c.L.rhs + i));
+    for (int k = i + 1; k < nv; ++k) s -= RC(c.d(c.L.M + k * (k + 1) / 2 + i)) * RC(c.d(c.L.rhs + k));
+    double x = double(s * RC(c.d(c.L.D + i)));
+    c.d(c.L.rhs + i) = x;
+    qdd[i] = x;
+    if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
+  }
+  return st;
+}
+
+// quaternion_derivative (src/util.rs:83-102) and the pose update of
+// euler_step / compute_new_q (src/integrators.rs:247-258,303-313).
+__device__ __forceinline__ void pose_advance(Col<double> q, int qo, const double* vel, double dt,
+                                             Col<double> qn) {
+  double x = q[qo], y = q[qo + 1], z = q[qo + 2], w = q[qo + 3];
+  double ox = vel[0], oy = vel[1], oz = vel[2];
+  double dw = 0.5 * (-x * ox - y * oy - z * oz);
+  double dx = 0.5 * (w * ox - z * oy + y * oz);
+  double dy = 0.5 * (z * ox + w * oy - x * oz);
+  double dz = 0.5 * (-y * ox + x * oy + w * oz);
+  // translation: t += dt · R(q_old) v_lin
+  M3<double> Rq = quat_to_mat<double>(x, y, z, w);
+  V3<double> td = mul(Rq, V3<double>{vel[3], vel[4], vel[5]});
+  double tx = q[qo + 4] + td.x * dt, ty = q[qo + 5] + td.y * dt, tz = q[qo + 6] + td.z * dt;
+  double nx = x + dx * dt, ny = y + dy * dt, nz = z + dz * dt, nw = w + dw * dt;
+  double inv = 1.0 / sqrt(nx * nx + ny * ny + nz * nz + nw * nw);
+  qn[qo] = nx * inv;
+  qn[qo + 1] = ny * inv;
+  qn[qo + 2] = nz * inv;
+  qn[qo + 3] = nw * inv;
+  qn[qo + 4] = tx;
+  qn[qo + 5] = ty;
+  qn[qo + 6] = tz;
+}
+
+// Advance positions: qn = q + dt·vel (per joint type), vel given as a column.
+template <typename R>
+__device__ __forceinline__ void advance_q(const LaneCtx<R>& c, Col<double> q, Col<double> vel,
+                                          double dt, Col<double> qn) {
+  for (int b = 0; b < c.nb; ++b) {
+    uint32_t w0 = c.w(2 * b);
+    int type = w0 & 15, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
+    if (type == 1 || type == 2) {
+      qn[qo] = q[qo] + vel[vo] * dt;
+    } else if (type == 3) {
+      double vv[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) vv[k] = vel[vo + k];
+      pose_advance(q, qo, vv, dt, qn);
+    }
+  }
+}
+
+template <typename R, typename RC>
+__device__ int lane_step(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<double> tau,
+                         bool have_tau, double dt, int integrator) {
+  const int nv = c.nv;
+  Col<double> f{&c.d(c.L.facc)};
+  Col<double> qs{&c.d(c.L.qs)}, vs{&c.d(c.L.vs)};
+  Col<double> tmp{&c.d(c.L.v0)};
+  Col<double> none{nullptr};
+  int st = 0;
+  if (integrator == 0) {  // semi-implicit Euler (src/integrators.rs:25-39,276-319)
+    st |= lane_dynamics<R, RC>(c, q, v, tau, have_tau, tmp, none, false);
+    if (st) return st;
+    for (int i = 0; i < nv; ++i) v[i] = v[i] + tmp[i] * dt;
+    advance_q(c, q, v, dt, q);
+    return st;
+  }
+  // Runge–Kutta: every stage starts from (q0, v0); positions use v0
+  // (src/integrators.rs:177-271).
+  // q is not written before the last stage, so it serves as q0.
+  Col<double> q0 = q;
+  Col<double> k1{&c.d(c.L.v0)};
+  st |= lane_dynamics<R, RC>(c, q, v, tau, have_tau, k1, none, false);
+  if (st) return st;
+  if (integrator == 1) {  // RK2
+    for (int i = 0; i < nv; ++i) vs[i] = v[i] + k1[i] * (dt / 2.0);
+    advance_q(c, q0, v, dt / 2.0, qs);
+    st |= lane_dynamics<R, RC>(c, qs, vs, tau, have_tau, k1, none, false);
+    if (st) return st;
+    advance_q(c, q0, v, dt, q);
+    for (int i = 0; i < nv; ++i) v[i] = v[i] + k1[i] * dt;
+    return st;
+  }
+  // RK4
+  for (int i = 0; i < nv; ++i) {
+    f[i] = k1[i];
+    vs[i] = v[i] + k1[i] * (dt / 2.0);
+  }
+  advance_q(c, q0, v, dt / 2.0, qs);
+  st |= lane_dynamics<R, RC>(c, qs, vs, tau, have_tau, k1, none, false);
+  if (st) return st;
+  for (int i = 0; i < nv; ++i) {
+    f[i] = f[i] + k1[i] * 2.0;
+    vs[i] = v[i] + k1[i] * (dt / 2.0);
+  }
+  // qs already equals q0 + dt/2 · v0
+  st |= lane_dynamics<R, RC>(c, qs, vs, tau, have_tau, k1, none, false);
+  if (st) return st;
+  for (int i = 0; i < nv; ++i) {
+    f[i] = f[i] + k1[i] * 2.0;
+    vs[i] = v[i] + k1[i] * dt;
+  }
+  advance_q(c, q0, v, dt, qs);
+  st |= lane_dynamics<R, RC>(c, qs, vs, tau, have_tau, k1, none, false);
+  if (st) return st;
+  for (int i = 0; i < nv; ++i) f[i] = (f[i] + k1[i]) / 6.0;
+  advance_q(c, q0, v, dt, q);
+  for (int i = 0; i < nv; ++i) v[i] = v[i] + f[i] * dt;
+  return st;
+}
+
+template <typename R>
+__device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackDesc& pd, int lane) {
+  LaneCtx<R> c;
+  c.lane = lane;
+  const int32_t* li = b.laneI + pd.lane * LANES + lane;
+  c.nb = li[1 * LANES];
+  c.nq = li[2 * LANES];
+  c.nv = li[3 * LANES];
+  c.nc = li[4 * LANES];
+  c.nh = li[5 * LANES];
+  c.model = li[6 * LANES];
+  c.chain = pd.chain;
+  c.W = b.topoW + pd.topo * 2 * LANES + lane;
+  c.T = RealTopo<R>::topo(b) + pd.topo * TOPO_D * LANES + lane;
+  c.CI = b.ctcI + pd.ctc * LANES + lane;
+  c.CD = RealTopo<R>::ctc(b) + pd.ctc * CTC_D * LANES + lane;
+  c.HD = RealTopo<R>::hs(b) + pd.hs * HS_D * LANES + lane;
+  c.L = scratch_layout(pd.nb, pd.nq, pd.nv, pd.nc);
+  c.sD = b.scratch + pd.scr * LANES + lane;
+  c.sR = reinterpret_cast<R*>(b.scratch + pd.scr * LANES) + lane;
+  return c;
+}
+
+// Control law before a step.
+template <typename R>
+__device__ __forceinline__ bool control(const LaneCtx<R>& c, const DeviceBatch& b,
+                                        const StepParams& p, int64_t inst, int64_t sidx, bool first,
+                                        Col<double> q, Col<double> v, Col<double> tin,
+                                        Col<double> tau) {
+  if (p.control == 1) {  // open loop
+    int rs = p.resample > 0 ? p.resample : 1;
+    if (first || sidx % rs == 0) {
+      int64_t block = sidx / rs;
+      for (int i = 0; i < c.nv; ++i) tau[i] = open_loop_tau(p.seed, inst, block, i, p.sigma);
+    }
+    return true;
+  }
+  if (p.control == 2) {  // PD on 1-DOF joints, zero elsewhere
+    for (int i = 0; i < c.nv; ++i) tau[i] = 0.0;
+    for (int bb = 0; bb < c.nb; ++bb) {
+      uint32_t w0 = c.w(2 * bb);
+      int type = w0 & 15, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
+      if (type == 1 || type == 2) tau[vo] = p.kp * (tin[vo] - q[qo]) + p.kd * -v[vo];
+    }
+    return true;
+  }
+  return p.tau_mode != 0;  // host torques live in tin
+}
+
+template <typename R, typename RCsmall>
+__global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams p) {
+  const int lane = threadIdx.x & 31;
+  const int warps_per_block = blockDim.x >> 5;
+  while (true) {
+    int pk = 0;
+    if (lane == 0) pk = atomicAdd(b.queue, 1);
+    pk = __shfl_sync(0xffffffffu, pk, 0);
+    if (pk >= b.npacks) break;
+    const PackDesc pd = b.packs[pk];
+    if (lane >= pd.count) continue;
+    LaneCtx<R> c = make_ctx<R>(b, pd, lane);
+    int32_t* status = b.status + (int64_t)pk * LANES + lane;
+    const int64_t inst = b.laneI[pd.lane * LANES + lane];
+    Col<double> q = col_at(b.q, pd.q, lane), v = col_at(b.v, pd.v, lane);
+    Col<double> tin = col_at(b.tau_in, pd.v, lane);
+    Col<double> tau{&c.d(c.L.tau)};
+    const bool small = c.nv <= 12;
+    for (int64_t s = 0; s < p.K; ++s) {
+      if (*status) break;
+      const int64_t sidx = p.step0 + s;
+      bool ht = control(c, b, p, inst, sidx, s == 0, q, v, tin, tau);
+      Col<double> tsrc = p.control == 0 ? tin : tau;
+      int st;
+      if (p.precision == 1 && small)
+        st = lane_step<R, RCsmall>(c, q, v, tsrc, ht, p.dt, p.integrator);
+      else
+        st = lane_step<R, double>(c, q, v, tsrc, ht, p.dt, p.integrator);
+      if (st) {
+        *status = st;
+        break;
+      }
+      for (int i = 0; i < c.nq; ++i)
+        if (!isfinite(q[i])) *status |= 1;
+      if (p.history && p.record_every > 0 && (s + 1) % p.record_every == 0) {
+        double* row = p.history + ((s + 1) / p.record_every - 1) * (b.nq_total + b.nv_total);
+        const int64_t* qm = b.qmap + pd.q * LANES + lane;
+        const int64_t* vm = b.vmap + pd.v * LANES + lane;
+        for (int i = 0; i < c.nq; ++i) row[qm[(size_t)i * LANES]] = q[i];
+        for (int i = 0; i < c.nv; ++i) row[b.nq_total + vm[(size_t)i * LANES]] = v[i];
+      }
+    }
+  }
+  (void)warps_per_block;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) dynamics_kernel(DeviceBatch b, StepParams p) {
+  const int lane = threadIdx.x & 31;
+  const int pk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (pk >= b.npacks) return;
+  const PackDesc pd = b.packs[pk];
+  if (lane >= pd.count) return;
+  LaneCtx<R> c = make_ctx<R>(b, pd, lane);
+  Col<double> q = col_at(b.q, pd.q, lane), v = col_at(b.v, pd.v, lane);
+  Col<double> tin = col_at(b.tau_in, pd.v, lane);
+  Col<double> qdd{&c.d(c.L.facc)};
+  Col<double> cf{&c.d(c.L.cf)};
+  for (int k = 0; k < 3 * c.nc; ++k) cf[k] = 0.0;
+  int st;
+  if (p.precision == 1 && c.nv <= 12)
+    st = lane_dynamics<R, float>(c, q, v, tin, p.tau_mode != 0, qdd, cf, true);
+  else
+    st = lane_dynamics<R, double>(c, q, v, tin, p.tau_mode != 0, qdd, cf, true);
+  b.status[(int64_t)pk * LANES + lane] |= st;
+  const int64_t* vm = b.vmap + pd.v * LANES + lane;
+  for (int i = 0; i < c.nv; ++i) p.qdd_out[vm[(size_t)i * LANES]] = qdd[i];
+  if (p.cforce_out) {
+    const int64_t* cm = b.cmap + pd.ctc * 3 * LANES + lane;
+    for (int k = 0; k < 3 * c.nc; ++k) p.cforce_out[cm[(size_t)k * LANES]] = cf[k];
+  }
+}
+
+__global__ void scatter_kernel(const int64_t* map, int64_t slots, const double* src, double* dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < slots;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t u = map[i];
+    if (u >= 0) dst[i] = src[u];
+  }
+}
+__global__ void gather_kernel(const int64_t* map, int64_t slots, const double* src, double* dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < slots;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t u = map[i];
+    if (u >= 0) dst[u] = src[i];
+  }
+}
+
+cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes_per_instance,
+                            int num_sms, cudaStream_t s) {
+  (void)lanes_per_instance;
+  cudaError_t e = cudaMemsetAsync(b.queue, 0, sizeof(int32_t), s);
+  if (e != cudaSuccess) return e;
+  const int threads = 128;
+  int per_sm = 0;
+  if (p.precision == 1)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, simulate_kernel<float, float>, threads, 0);
+  else
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, simulate_kernel<double, double>, threads, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  int64_t want = (b.npacks + (threads / 32) - 1) / (threads / 32);
+  int64_t grid = (int64_t)num_sms * per_sm;
+  if (grid > want) grid = want;
+  if (grid < 1) grid = 1;
+  if (p.precision == 1)
+    simulate_kernel<float, float><<<(unsigned)grid, threads, 0, s>>>(b, p);
+  else
+    simulate_kernel<double, double><<<(unsigned)grid, threads, 0, s>>>(b, p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dynamics(const DeviceBatch& b, const StepParams& p, cudaStream_t s) {
+  const int threads = 128;
+  unsigned grid = (unsigned)((b.npacks + 3) / 4);
+  if (grid == 0) return cudaSuccess;
+  if (p.precision == 1)
+    dynamics_kernel<float><<<grid, threads, 0, s>>>(b, p);
+  else
+    dynamics_kernel<double><<<grid, threads, 0, s>>>(b, p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const int64_t* map, int64_t slots, const double* src, double* dst,
+                           cudaStream_t s) {
+  if (slots <= 0) return cudaSuccess;
+  int64_t blocks = (slots + 255) / 256;
+  if (blocks > 65535) blocks = 65535;
+  scatter_kernel<<<(unsigned)blocks, 256, 0, s>>>(map, slots, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_gather(const int64_t* map, int64_t slots, const double* src, double* dst,
+                          cudaStream_t s) {
+  if (slots <= 0) return cudaSuccess;
+  int64_t blocks = (slots + 255) / 256;
+  if (blocks > 65535) blocks = 65535;
+  gather_kernel<<<(unsigned)blocks, 256, 0, s>>>(map, slots, src, dst);
+  return cudaGetLastError();
+}
+
+}  // namespace gpb

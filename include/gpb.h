@@ -1,0 +1,281 @@
+/*
+ * gpb.h — C ABI of the GB300-native batched rigid-body step.
+ *
+ * The library batches the step that gorilla-physics' `simulate` loop runs for
+ * one mechanism (src/simulate.rs:20-112) over tens of thousands of independent
+ * mechanisms on one GPU:
+ *   - forward kinematics and world-frame twists (src/mechanism.rs:153-188,
+ *     src/spatial/twist.rs:176-204),
+ *   - the CRBA joint-space mass matrix (src/mechanism.rs:592-696),
+ *   - point / sphere vs half-space contact forces (src/contact.rs:97-128,
+ *     260-338, src/collision/halfspace.rs:39-44),
+ *   - the RNEA dynamics bias (src/dynamics.rs:41-251, src/spatial/wrench.rs:96-126),
+ *   - the solve for q̈ (src/dynamics.rs:255-276; Cholesky instead of LU),
+ *   - semi-implicit Euler / RK2 / RK4 (src/integrators.rs:25-39,177-319).
+ *
+ * Conventions
+ *   - Every entry point returns 0 on success or a negative GPB_E_* code.  The
+ *     message of the last failure on the calling thread is gpb_last_error().
+ *     Per-instance numerical faults (non-finite state, a mass matrix that is not
+ *     positive definite) never abort a call: they are recorded in the per-instance
+ *     status array (gpb_batch_status) and that instance is frozen.
+ *   - Host buffers passed in are copied; device buffers are owned by the library.
+ *   - Body / joint numbering inside one mechanism follows MechanismState
+ *     (src/mechanism.rs:37-58): joint i has child body i, bodies are 1-based,
+ *     body 0 is the world, and parent(i) < i.
+ *   - Per-instance q and v are flattened exactly like the reference's
+ *     `to_float_dvec` (src/joint/mod.rs:208-303): revolute / prismatic 1 value,
+ *     floating q = [qx,qy,qz,qw,tx,ty,tz], floating v = [ωx,ωy,ωz,vx,vy,vz] in the
+ *     body frame, fixed 0 values.  A batch stores instances back to back in the
+ *     order they were given; gpb_batch_layout reports each instance's offsets.
+ *   - One context drives one CUDA device on one stream and is used from one
+ *     host thread at a time.  Several contexts may share a device.
+ */
+#ifndef GPB_H
+#define GPB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPB_ABI_VERSION 1
+
+/* ---- return codes ---------------------------------------------------- */
+#define GPB_OK 0
+#define GPB_E_INVAL (-1)   /* bad argument / malformed mechanism            */
+#define GPB_E_NOMEM (-2)   /* device or host allocation failed              */
+#define GPB_E_CUDA (-3)    /* a CUDA runtime call failed                    */
+#define GPB_E_TIMEOUT (-4) /* a bounded device wait ran out                 */
+#define GPB_E_RANGE (-5)   /* size beyond a documented limit                */
+#define GPB_E_STATE (-6)   /* call not valid in the object's current state  */
+
+/* ---- per-instance status bits (gpb_batch_status) ---------------------- */
+#define GPB_ST_OK 0
+#define GPB_ST_NONFINITE 1 /* q, v, q̈ or a contact force became NaN/Inf   */
+#define GPB_ST_CHOL_FAIL 2 /* mass matrix not positive definite            */
+
+/* ---- enums ------------------------------------------------------------ */
+/* Joint kinds of src/joint/mod.rs:21-27. */
+enum gpb_joint_type {
+  GPB_JOINT_FIXED = 0,
+  GPB_JOINT_REVOLUTE = 1,
+  GPB_JOINT_PRISMATIC = 2,
+  GPB_JOINT_FLOATING = 3
+};
+
+/* Continuous integrators of src/integrators.rs:17-23 (the velocity-stepping
+ * variants solve a conic program and are not part of this library). */
+enum gpb_integrator {
+  GPB_SEMI_IMPLICIT_EULER = 0,
+  GPB_RUNGE_KUTTA_2 = 1,
+  GPB_RUNGE_KUTTA_4 = 2
+};
+
+/* GPB_FP64: every quantity in FP64 (the drop-in).  GPB_MIXED: sweeps, contact
+ * and mass-matrix build in FP32; FP64 position/quaternion accumulator; FP64
+ * Cholesky when n > 12. */
+enum gpb_precision { GPB_FP64 = 0, GPB_MIXED = 1 };
+
+/* GPB_HUNT_CROSSLEY: src/contact.rs:260-338 (k = k_p k_h/(k_p+k_h), k_h = 50e3,
+ * π = max(λ z^1.5 ż + k z^1.5, 0), λ = 1.5 α k).
+ * GPB_LINEAR_SPRING_DAMPER: π = max(k z + c ż, 0) with the same friction. */
+enum gpb_contact_model { GPB_HUNT_CROSSLEY = 0, GPB_LINEAR_SPRING_DAMPER = 1 };
+
+/* Device-side control law evaluated before every step. */
+enum gpb_control {
+  GPB_CONTROL_HOST_TAU = 0,    /* τ given by the caller (constant over the call) */
+  GPB_CONTROL_OPEN_LOOP = 1,   /* τ ~ N(0, σ²) per DOF, resampled every R steps  */
+  GPB_CONTROL_PD = 2           /* τ = kp (q* − q) − kd v on 1-DOF joints           */
+};
+
+/* ---- mechanism tables (flattened structure of arrays) ----------------- */
+/*
+ * All instances of a batch are described by one gpb_model.  Instance i owns
+ * joints/bodies [joint_offset[i], joint_offset[i+1]), contact points
+ * [contact_offset[i], contact_offset[i+1]) and half-spaces
+ * [halfspace_offset[i], halfspace_offset[i+1]).
+ *
+ * joint_type[j]     gpb_joint_type
+ * joint_parent[j]   parent body number within the instance (0 = world), < own number
+ * joint_iso[7j..]   init_iso of the joint: quaternion (qx,qy,qz,qw) then translation
+ *                   (transform from the child body frame to the parent frame,
+ *                   src/joint/revolute.rs:18-19)
+ * joint_axis[3j..]  unit axis in the child frame (revolute / prismatic)
+ * joint_spring[2j..] prismatic spring (k, rest length); k == 0 means no spring
+ *                   (src/joint/prismatic.rs:12-16, src/dynamics.rs:298-315)
+ * body_inertia[10j..] mass, cross_part (m·com, 3), moment about the frame origin
+ *                   (Jxx, Jyy, Jzz, Jxy, Jxz, Jyz)  (src/inertia.rs:31-37)
+ * contact_body[c]   body number (1-based) the point is fixed to
+ * contact_params[6c..] location in the body frame (3), k, radius, damping.
+ *                   radius 0 is the reference ContactPoint (src/contact.rs:16-21);
+ *                   radius > 0 is a sphere: penetration r − d, applied at the
+ *                   sphere point nearest the half-space.
+ * halfspace_params[8h..] point (3), outward unit normal (3), alpha, mu
+ *                   (src/collision/halfspace.rs:6-11)
+ * contact_model[i]  gpb_contact_model of instance i
+ */
+typedef struct gpb_model {
+  int64_t n_instances;
+  const int32_t* joint_offset;     /* [n_instances + 1] */
+  const int32_t* joint_type;
+  const int32_t* joint_parent;
+  const double* joint_iso;
+  const double* joint_axis;
+  const double* joint_spring;
+  const double* body_inertia;
+  const int32_t* contact_offset;   /* [n_instances + 1] */
+  const int32_t* contact_body;
+  const double* contact_params;
+  const int32_t* halfspace_offset; /* [n_instances + 1] */
+  const double* halfspace_params;
+  const int32_t* contact_model;    /* [n_instances] */
+} gpb_model;
+
+/* Limits of one instance. */
+#define GPB_MAX_BODIES 64
+#define GPB_MAX_DOF 64
+#define GPB_MAX_CONTACTS 64
+#define GPB_MAX_HALFSPACES 4
+
+/* ---- library / context ------------------------------------------------ */
+typedef struct gpb_ctx gpb_ctx;
+typedef struct gpb_batch gpb_batch;
+
+int gpb_abi_version(void);
+const char* gpb_last_error(void);
+
+/* Creates a context on CUDA device `device` with its own stream. */
+int gpb_create(int device, gpb_ctx** out);
+int gpb_destroy(gpb_ctx* ctx);
+
+/* ---- batches ----------------------------------------------------------- */
+/*
+ * Validates and uploads the mechanisms of `model` (one per instance), builds
+ * the structure-of-arrays topology tables and allocates per-instance state
+ * (initially q = joint zero / identity pose, v = 0, like MechanismState::new,
+ * src/mechanism.rs:62-148).  Replaces MechanismState::new for a whole slice.
+ */
+int gpb_batch_create(gpb_ctx* ctx, const gpb_model* model, gpb_batch** out);
+int gpb_batch_destroy(gpb_batch* batch);
+
+/* Per-instance offsets into the flattened q / v vectors ([n+1] each) and the
+ * totals.  Any pointer may be NULL. */
+int gpb_batch_layout(const gpb_batch* batch, int64_t* q_offset, int64_t* v_offset,
+                     int64_t* nq_total, int64_t* nv_total);
+
+/* Replaces MechanismState::update(q, v) (src/mechanism.rs:209-214) for every
+ * instance: q and v hold nq_total / nv_total doubles. */
+int gpb_set_state(gpb_batch* batch, const double* q, const double* v);
+int gpb_get_state(gpb_batch* batch, double* q, double* v);
+
+/* ---- the hot path ------------------------------------------------------ */
+/*
+ * dynamics_continuous (src/dynamics.rs:322-364) for every instance at its
+ * current state: writes q̈ (nv_total doubles) and, if `contact_force` is not
+ * NULL, the world-frame force of every contact point (3 per point, summed over
+ * half-spaces).  `tau` (nv_total doubles) may be NULL for zero torque
+ * (src/simulate.rs:26-37).
+ */
+int gpb_dynamics(gpb_batch* batch, const double* tau, int precision, double* qdd,
+                 double* contact_force);
+
+/*
+ * step (src/simulate.rs:20-83) for every instance: one integrator step of
+ * size dt with joint torques `tau` (NULL = zero).  State stays on the device.
+ */
+int gpb_step(gpb_batch* batch, double dt, const double* tau, int integrator,
+             int precision);
+
+/* Device-side control for gpb_simulate. */
+typedef struct gpb_control_params {
+  int32_t mode;          /* gpb_control */
+  uint32_t seed;         /* OPEN_LOOP: stream seed (Philox4x32-10 key word 1) */
+  int32_t resample_every;/* OPEN_LOOP: steps between torque draws (≥ 1) */
+  double sigma;          /* OPEN_LOOP: standard deviation of τ */
+  double kp, kd;         /* PD gains */
+  const double* tau;     /* HOST_TAU: nv_total doubles (NULL = zero);
+                            PD: per-DOF target q* (nv_total doubles, only the
+                            1-DOF joints are used) */
+} gpb_control_params;
+
+/*
+ * K steps of `simulate` (src/simulate.rs:87-112) for every instance, with the
+ * control law evaluated on the device each step.  The step counter `step0` is
+ * the global index of the first step (it keys the open-loop torque draws, so a
+ * horizon split over several calls draws the same torques).  If `history` is not
+ * NULL, q and v after every `record_every`-th step are written to it as
+ * [K / record_every][nq_total + nv_total] doubles.
+ */
+int gpb_simulate(gpb_batch* batch, double dt, int64_t K, int64_t step0,
+                 int integrator, int precision, const gpb_control_params* control,
+                 int64_t record_every, double* history);
+
+/* Step count of the reference loop `while t < final_time { …; t += dt }`
+ * (src/simulate.rs:97-109), float accumulation included. */
+int64_t gpb_simulate_steps(double final_time, double dt);
+
+/* Per-instance status words (GPB_ST_* bits), n_instances int32. */
+int gpb_batch_status(gpb_batch* batch, int32_t* status);
+/* Clears all status words (e.g. after the caller repaired the state). */
+int gpb_batch_clear_status(gpb_batch* batch);
+
+/* Waits for all work of the context's stream. */
+int gpb_synchronize(gpb_ctx* ctx);
+
+/* ---- kernel mapping ---------------------------------------------------- */
+/*
+ * Lanes cooperating on one instance: 1 (32 instances per warp, serial sweeps),
+ * or 0 = let the library choose per size class (the autotuned default).
+ */
+int gpb_batch_set_mapping(gpb_batch* batch, int lanes_per_instance);
+
+/* Number of this library's kernel launches issued by the context so far. */
+int64_t gpb_launch_count(const gpb_ctx* ctx);
+
+/* Device time (ms, CUDA events on the context's stream) of the last
+ * gpb_simulate / gpb_step kernel; waits for it.  −1 if none ran. */
+double gpb_last_launch_ms(gpb_ctx* ctx);
+
+/* ---- synthetic configurations ------------------------------------------ */
+/*
+ * Seeded builders of the benchmark mechanisms (all draws from Philox4x32-10
+ * keyed by (instance, seed)):
+ *   0  acrobot: 2 revolute links about y, lengths 1 and 2 m, 1 kg, rod inertia
+ *   1  serial revolute chain, n ~ U{2..48}, axes U{x,y,z}, l ~ U(0.2,1), m ~ U(0.5,2)
+ *   2  free-floating cube, side U(0.2,1) m, 1000 kg/m³, 8 corner contacts, μ ~ U(0.3,1)
+ *   3  quadruped: floating 0.6×0.3×0.15 m torso (10 kg), 4 legs × 3 revolute
+ *      joints, 0.25 m / 1 kg links, foot spheres r = 0.02 m
+ * gpb_config_sizes returns the table sizes; gpb_config_build fills caller-owned
+ * arrays laid out as gpb_model (offsets included) plus the initial q / v and,
+ * for config 3, the per-DOF PD targets (`aux`, nv doubles; may be NULL).
+ * `contact_model` selects the normal-force law for configs 2 and 3.
+ */
+int gpb_config_sizes(int config, int64_t n_instances, uint32_t seed, int64_t* n_joints,
+                     int64_t* n_contacts, int64_t* n_halfspaces, int64_t* nq, int64_t* nv);
+int gpb_config_build(int config, int64_t n_instances, uint32_t seed, int contact_model,
+                     int32_t* joint_offset, int32_t* joint_type, int32_t* joint_parent,
+                     double* joint_iso, double* joint_axis, double* joint_spring,
+                     double* body_inertia, int32_t* contact_offset, int32_t* contact_body,
+                     double* contact_params, int32_t* halfspace_offset,
+                     double* halfspace_params, int32_t* contact_model_out, double* q0,
+                     double* v0, double* aux);
+
+/* The open-loop torque draw for (seed, instance, draw block, dof): the value
+ * the device uses, exported so that callers can replay a horizon. */
+double gpb_open_loop_tau(uint32_t seed, int64_t instance, int64_t block, int32_t dof,
+                         double sigma);
+
+/* ---- measurement ------------------------------------------------------- */
+/* FMA throughput of the FP64 (GPB_FP64) or FP32 (GPB_MIXED) pipe in TFLOP/s,
+ * counting 2 flops per fused multiply-add of the `active_lanes` (1..32) lanes
+ * of each warp that issue: the roofline denominator of the batched step. */
+int gpb_fma_peak(int device, int precision, int active_lanes, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPB_H */

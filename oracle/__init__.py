@@ -1,0 +1,156 @@
+"""TEST INFRASTRUCTURE — the CPU oracle (FP64 restatement of gorilla-physics'
+continuous step).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline may use it, and only as the checker / baseline, never as a product
+path.
+
+Functions take a ``gpb.Model`` and one instance's flattened q / v / τ.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent
+LIB = HERE / "liboracle.so"
+SRC = HERE / "gpb_oracle.cpp"
+
+P_f64 = C.POINTER(C.c_double)
+P_i64 = C.POINTER(C.c_int64)
+P_i32 = C.POINTER(C.c_int32)
+
+LU, CHOLESKY = 0, 1
+
+
+def build(force: bool = False) -> Path:
+    """g++ -O2 -ffp-contract=off (x86 and Arm agree bit for bit)."""
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime,
+                                                              (REPO / "include/gpb.h").stat().st_mtime):
+        tmp = LIB.with_suffix(".so.tmp")
+        subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
+                        "-I", str(REPO / "include"), str(SRC), "-o", str(tmp), "-lpthread"],
+                       check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        vp = C.c_void_p
+        L.oracle_dims.argtypes = [vp, C.c_int64, P_i32, P_i32, P_i32]
+        L.oracle_dynamics.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_int, P_f64, P_f64]
+        L.oracle_mass_matrix.argtypes = [vp, C.c_int64, P_f64, P_f64]
+        L.oracle_energy.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, P_f64]
+        L.oracle_step.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_double, C.c_int, C.c_int]
+        L.oracle_open_loop_tau.argtypes = [C.c_uint32, C.c_int64, C.c_int64, C.c_int32, C.c_double]
+        L.oracle_open_loop_tau.restype = C.c_double
+        L.oracle_simulate.argtypes = [vp, C.c_int64, P_f64, P_f64, C.c_double, C.c_int64,
+                                      C.c_int64, C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_int,
+                                      C.c_double, C.c_double, C.c_double, P_f64, C.c_int64, P_f64]
+        L.oracle_simulate_batch.argtypes = [vp, C.c_int64, C.c_int64, P_i64, P_i64, P_f64, P_f64,
+                                            C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_int,
+                                            C.c_int, C.c_uint32, C.c_int, C.c_double, C.c_double,
+                                            C.c_double, P_f64, C.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(P_f64)
+
+
+def _m(model):
+    return C.cast(C.pointer(model.struct()), C.c_void_p)
+
+
+def dims(model, i):
+    nq, nv, nc = C.c_int32(), C.c_int32(), C.c_int32()
+    rc = lib().oracle_dims(_m(model), i, C.byref(nq), C.byref(nv), C.byref(nc))
+    if rc:
+        raise ValueError(f"oracle: malformed instance {i}")
+    return nq.value, nv.value, nc.value
+
+
+def dynamics(model, i, q, v, tau=None, solver=LU, contact_forces=False):
+    """q̈ (and contact forces) of instance i; returns (qdd, status[, cforce])."""
+    nq, nv, nc = dims(model, i)
+    q = np.ascontiguousarray(q, float)
+    v = np.ascontiguousarray(v, float)
+    t = None if tau is None else np.ascontiguousarray(tau, float)
+    qdd = np.zeros(max(nv, 1))
+    cf = np.zeros(max(3 * nc, 1))
+    st = lib().oracle_dynamics(_m(model), i, _p(q), _p(v), _p(t), solver, _p(qdd), _p(cf))
+    if contact_forces:
+        return qdd[:nv], st, cf[:3 * nc]
+    return qdd[:nv], st
+
+
+def mass_matrix(model, i, q):
+    nq, nv, _ = dims(model, i)
+    H = np.zeros((max(nv, 1), max(nv, 1)))
+    lib().oracle_mass_matrix(_m(model), i, _p(np.ascontiguousarray(q, float)), _p(H))
+    return H[:nv, :nv]
+
+
+def energy(model, i, q, v):
+    ke, pe = C.c_double(), C.c_double()
+    lib().oracle_energy(_m(model), i, _p(np.ascontiguousarray(q, float)),
+                        _p(np.ascontiguousarray(v, float)), C.byref(ke), C.byref(pe))
+    return ke.value, pe.value
+
+
+def step(model, i, q, v, dt, tau=None, integrator=0, solver=LU):
+    q = np.array(q, float)
+    v = np.array(v, float)
+    t = None if tau is None else np.ascontiguousarray(tau, float)
+    st = lib().oracle_step(_m(model), i, _p(q), _p(v), _p(t), dt, integrator, solver)
+    return q, v, st
+
+
+def open_loop_tau(seed, inst, block, dof, sigma=1.0):
+    return lib().oracle_open_loop_tau(seed, inst, block, dof, sigma)
+
+
+CONTROL = {"host": 0, "open_loop": 1, "pd": 2}
+
+
+def simulate(model, i, q, v, dt, K, integrator=0, solver=LU, control="host", ctl=None, seed=0,
+             resample_every=10, sigma=1.0, kp=0.0, kd=0.0, step0=0, record_every=0):
+    """K steps of instance i; returns (q, v, status, history)."""
+    nq, nv, _ = dims(model, i)
+    q = np.array(q, float)
+    v = np.array(v, float)
+    c = None if ctl is None else np.ascontiguousarray(ctl, float)
+    hist = np.zeros(max((K // record_every) * (nq + nv), 1)) if record_every > 0 else None
+    st = lib().oracle_simulate(_m(model), i, _p(q), _p(v), dt, K, step0, integrator, solver,
+                               CONTROL[control], seed, resample_every, sigma, kp, kd, _p(c),
+                               record_every, _p(hist))
+    if hist is not None:
+        hist = hist[:(K // record_every) * (nq + nv)].reshape(K // record_every, nq + nv)
+    return q, v, st, hist
+
+
+def simulate_batch(model, q_all, v_all, dt, K, integrator=0, solver=LU, control="host",
+                   ctl_all=None, seed=0, resample_every=10, sigma=1.0, kp=0.0, kd=0.0, step0=0,
+                   begin=0, end=None, threads=1):
+    """K steps of instances [begin, end) in place on `threads` host threads."""
+    qo, vo, _ = model.offsets()
+    end = model.n if end is None else end
+    c = None if ctl_all is None else np.ascontiguousarray(ctl_all, float)
+    rc = lib().oracle_simulate_batch(_m(model), begin, end, qo.ctypes.data_as(P_i64),
+                                     vo.ctypes.data_as(P_i64), _p(q_all), _p(v_all), dt, K, step0,
+                                     integrator, solver, CONTROL[control], seed, resample_every,
+                                     sigma, kp, kd, _p(c), threads)
+    if rc:
+        raise ValueError("oracle: malformed model")

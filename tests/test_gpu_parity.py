@@ -1,0 +1,225 @@
+"""GPU parity: the CUDA kernels (through the C ABI) against the oracle.
+
+Tolerances
+  * FP64 form, one dynamics evaluation: ‖q̈_gpu − q̈_ref‖∞ ≤ 1e-10 · max(‖q̈_ref‖∞, 1)
+    against the oracle's Cholesky solve, and the same bound scaled by the
+    instance's condition number against the reference's LU solve (the two
+    factorisations differ by ≈ cond(M)·ε).
+  * Contact forces: 1e-10 relative to max(|f|, 1).
+  * One integrator step: q, v within 1e-12 · max(|x|, 1).
+  * 200-step trajectories: within 1e-8 · max(|x|, 1) (chaotic chains amplify
+    round-off; the bound holds over this horizon at these step sizes).
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+import gpb
+import oracle
+from gpb import Batch, HalfSpace, Model
+from tests.golden import kats
+
+pytestmark = pytest.mark.gpu
+G = 9.81
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)) if b.size else 0.0, 1.0)
+
+
+def slices(M):
+    qo, vo, co = M.offsets()
+    return qo, vo, co
+
+
+# ---------------------------------------------------------------------------
+# single evaluations
+
+def test_known_answers_fp64(ctx):
+    cases = kats.dynamics_cases()
+    mechs = [c[1] for c in cases]
+    B = Batch(mechs, ctx)
+    q = np.concatenate([np.asarray(c[2], float) for c in cases])
+    v = np.concatenate([np.asarray(c[3], float) for c in cases])
+    tau = np.concatenate([np.asarray(c[4], float) for c in cases])
+    B.update(q, v)
+    qdd = B.dynamics_continuous(tau)
+    o = 0
+    for name, mech, _, _, _, expected, tol, src in cases:
+        n = len(expected)
+        np.testing.assert_allclose(qdd[o:o + n], expected, rtol=0, atol=tol, err_msg=f"{name} {src}")
+        o += n
+    assert np.all(B.status() == 0)
+
+
+@pytest.mark.parametrize("config,n,model", [(0, 256, 1), (1, 512, 1), (2, 256, 1), (2, 256, 0),
+                                            (3, 96, 1), (3, 96, 0)])
+def test_config_dynamics_fp64(ctx, config, n, model):
+    M, q0, v0, aux = Model.from_config(config, n, seed=5, contact_model=model)
+    qo, vo, co = slices(M)
+    rng = np.random.default_rng(config)
+    if config in (2, 3):
+        # push some instances into the ground so contacts are active
+        q0 = q0.copy()
+        for i in range(n):
+            q0[qo[i] + 6] = rng.uniform(-0.01, 0.5) if config == 2 else rng.uniform(0.38, 0.45)
+    tau = rng.normal(size=v0.size)
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    qdd, cf = B.dynamics_continuous(tau, contact_forces=True)
+    worst_chol = worst_lu = worst_cf = 0.0
+    active = 0
+    for i in range(n):
+        qi, vi, ti = q0[qo[i]:qo[i + 1]], v0[vo[i]:vo[i + 1]], tau[vo[i]:vo[i + 1]]
+        ref_c, st, cf_ref = oracle.dynamics(M, i, qi, vi, ti, solver=oracle.CHOLESKY, contact_forces=True)
+        ref_l, _ = oracle.dynamics(M, i, qi, vi, ti, solver=oracle.LU)
+        g = qdd[vo[i]:vo[i + 1]]
+        worst_chol = max(worst_chol, rel_err(g, ref_c))
+        H = oracle.mass_matrix(M, i, qi)
+        cond = np.linalg.cond(H)
+        worst_lu = max(worst_lu, rel_err(g, ref_l) / max(cond, 1.0))
+        gcf = cf[3 * co[i]:3 * co[i + 1]]
+        worst_cf = max(worst_cf, rel_err(gcf, cf_ref))
+        active += int(np.any(cf_ref != 0))
+    assert worst_chol <= 1e-10, worst_chol
+    assert worst_lu <= 1e-12, worst_lu
+    assert worst_cf <= 1e-10, worst_cf
+    if config in (2, 3):
+        assert active > n // 4
+    assert np.all(B.status() == 0)
+
+
+def test_mixed_precision_error(ctx):
+    """MIXED on C1 chains: q̈ error against FP64 stays small."""
+    M, q0, v0, _ = Model.from_config(1, 512, seed=9)
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    a = B.dynamics_continuous(None, precision=gpb.FP64)
+    b = B.dynamics_continuous(None, precision=gpb.MIXED)
+    qo, vo, _ = M.offsets()
+    errs = [rel_err(b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]) for i in range(M.n)]
+    assert np.all(np.isfinite(b))
+    assert np.median(errs) < 1e-3, np.median(errs)
+
+
+# ---------------------------------------------------------------------------
+# integrators
+
+@pytest.mark.parametrize("integrator", [gpb.SEMI_IMPLICIT_EULER, gpb.RUNGE_KUTTA_2, gpb.RUNGE_KUTTA_4])
+@pytest.mark.parametrize("config", [0, 1, 2, 3])
+def test_one_step(ctx, integrator, config):
+    n = 64
+    M, q0, v0, _ = Model.from_config(config, n, seed=3)
+    qo, vo, _ = slices(M)
+    dt = {0: 1e-3, 1: 5e-4, 2: 1e-4, 3: 2e-4}[config]
+    tau = np.random.default_rng(1).normal(size=v0.size)
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    B.step(dt, tau, integrator)
+    q, v = B.state()
+    for i in range(n):
+        qr, vr, st = oracle.step(M, i, q0[qo[i]:qo[i + 1]], v0[vo[i]:vo[i + 1]], dt,
+                                 tau[vo[i]:vo[i + 1]], integrator, solver=oracle.CHOLESKY)
+        assert rel_err(q[qo[i]:qo[i + 1]], qr) < 1e-12
+        assert rel_err(v[vo[i]:vo[i + 1]], vr) < 1e-12
+
+
+@pytest.mark.parametrize("config,control", [(0, "host"), (1, "open_loop"), (2, "host"), (3, "pd")])
+def test_trajectory_200_steps(ctx, config, control):
+    n = 64
+    M, q0, v0, aux = Model.from_config(config, n, seed=21)
+    qo, vo, _ = slices(M)
+    dt = {0: 1e-3, 1: 5e-4, 2: 1e-4, 3: 2e-4}[config]
+    kw = dict(seed=77, resample_every=10, sigma=1.0, kp=50.0, kd=2.0)
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    ctl = aux if control == "pd" else None
+    hist = B.simulate_steps(200, dt, gpb.SEMI_IMPLICIT_EULER, gpb.FP64, control, tau=ctl,
+                            record_every=50, **kw)
+    q, v = B.state()
+    for i in range(n):
+        c = None if ctl is None else ctl[vo[i]:vo[i + 1]]
+        qr, vr, st, hr = oracle.simulate(M, i, q0[qo[i]:qo[i + 1]], v0[vo[i]:vo[i + 1]], dt, 200,
+                                         0, oracle.CHOLESKY, control, c, record_every=50, **kw)
+        assert rel_err(q[qo[i]:qo[i + 1]], qr) < 1e-8, i
+        assert rel_err(v[vo[i]:vo[i + 1]], vr) < 1e-8, i
+        nq = qo[i + 1] - qo[i]
+        for r in range(4):
+            assert rel_err(hist[r, qo[i]:qo[i + 1]], hr[r, :nq]) < 1e-8
+    assert np.all(B.status() == 0)
+
+
+def test_split_horizon_equals_one_call(ctx):
+    """Open-loop draws are keyed by the global step: 2 × 100 steps == 200 steps."""
+    M, q0, v0, _ = Model.from_config(1, 64, seed=4)
+    A = Batch(M, ctx)
+    A.update(q0, v0)
+    A.simulate_steps(200, 5e-4, control="open_loop", seed=5)
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    B.simulate_steps(100, 5e-4, control="open_loop", seed=5)
+    B.simulate_steps(100, 5e-4, control="open_loop", seed=5, step0=100)
+    np.testing.assert_array_equal(A.q, B.q)
+    np.testing.assert_array_equal(A.v, B.v)
+
+
+# ---------------------------------------------------------------------------
+# reference trajectory tests through the GPU (physical outcomes)
+
+def test_reference_trajectories_on_gpu(ctx):
+    m, l = 5.0, 7.0
+    rod = kats.pendulum(m, (0, m * l * l / 3, m * l * l / 3), (m * l / 2, 0, 0))
+    B = Batch([rod], ctx)
+    qs, vs = gpb.simulate(B, 10.0, 0.001, tau=[0.0])
+    assert abs(qs[:, 0].max() - math.pi) < 1e-2  # simulate.rs:129-174
+    E = m * G * l / 2 * (-math.sin(qs[-1, 0])) + 0.5 * (m * l * l / 3) * vs[-1, 0] ** 2
+    assert abs(E) < 1e-1
+
+    c = kats.cube(3.0, 1.0)
+    c.add_halfspace(HalfSpace.new((0, 0, 1), -10.0))
+    B = Batch([c], ctx)
+    B.update([0, 0, 0, 1, 0, 0, 0], [1] * 6)
+    B.simulate_steps(gpb.simulate_steps(5.0, 1e-3), 1e-3, gpb.RUNGE_KUTTA_4)
+    assert abs(B.q[6] + 9.5) < 1e-2  # contact.rs:408-441
+
+    s = kats.sphere_point()
+    s.add_halfspace(HalfSpace.new((0, 0, 1), -0.3, 1.0, 0.5))
+    B = Batch([s], ctx)
+    B.update([0, 0, 0, 1, 0, 0, 0], [0, 0, 0, 2.0, 0, 0])
+    B.simulate_steps(gpb.simulate_steps(2.0, 1e-3), 1e-3, gpb.RUNGE_KUTTA_4)
+    th = math.sqrt(0.3 * 2 / G)
+    vx = 2.0 - G * th * 0.5
+    ts = vx / (G * 0.5)
+    assert abs(B.q[4] - (th * 2.0 + vx * ts - G * 0.5 * ts * ts / 2)) < 1e-2  # contact.rs:607-675
+
+
+# ---------------------------------------------------------------------------
+# failure handling: per-instance status, never a fault
+
+def test_nonfinite_state_is_flagged_and_frozen(ctx):
+    M, q0, v0, _ = Model.from_config(0, 64, seed=1)
+    B = Batch(M, ctx)
+    q0 = q0.copy()
+    q0[2 * 5] = np.nan
+    B.update(q0, v0)
+    B.simulate_steps(10, 1e-3)
+    st = B.status()
+    assert st[5] & 1 and np.all(np.delete(st, 5) == 0)
+    q, _ = B.state()
+    assert np.isnan(q[10])
+
+
+def test_non_spd_mass_matrix_is_flagged(ctx):
+    M, q0, v0, _ = Model.from_config(0, 32, seed=1)
+    M.body_inertia[10 * 2 * 3:10 * 2 * 3 + 10] *= -1.0  # instance 3: negative inertia
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    q_before = B.q.copy()
+    B.simulate_steps(5, 1e-3)
+    st = B.status()
+    assert st[3] & 2
+    np.testing.assert_array_equal(B.q[6:8], q_before[6:8])  # frozen
+    assert np.sum(st != 0) == 1
