@@ -134,8 +134,12 @@ void build_one(int config, int64_t inst, uint32_t seed, int contact_model, Build
       B.qv(q, v);
     }
   } else if (config == 1) {  // serial chain
+    // Each rod points away from its joint perpendicular to the joint's own axis
+    // (axis x or y: rod along −z; axis z: rod along −x), so that no joint spins
+    // its own link about the link's long axis (a near-zero inertia that makes
+    // the chain ill-posed).  Rod radius 0.05·l.
     int n = d.integer(2, 48);
-    double prev_l = 0.0;
+    double prev[3] = {0, 0, 0};
     for (int k = 0; k < n; ++k) {
       int a = d.integer(0, 2);
       double ax[3] = {0, 0, 0};
@@ -143,10 +147,18 @@ void build_one(int config, int64_t inst, uint32_t seed, int contact_model, Build
       double l = d.uniform(0.2, 1.0);
       double m = d.uniform(0.5, 2.0);
       double c[3], mo[6];
-      rod(m, l, 0.05 * l, c, mo);
-      double t[3] = {0, 0, -prev_l};
-      B.joint(GPB_JOINT_REVOLUTE, k, IDQ, t, ax, m, c, mo);
-      prev_l = l;
+      rod(m, l, 0.05 * l, c, mo);  // along −z
+      if (a == 2) {                // rotate the rod to −x: swap the x and z roles
+        c[0] = c[2];
+        c[2] = 0.0;
+        double jx = mo[0];
+        mo[0] = mo[2];
+        mo[2] = jx;
+      }
+      B.joint(GPB_JOINT_REVOLUTE, k, IDQ, prev, ax, m, c, mo);
+      prev[0] = a == 2 ? -l : 0.0;
+      prev[1] = 0.0;
+      prev[2] = a == 2 ? 0.0 : -l;
     }
     for (int k = 0; k < n; ++k) {
       double q = d.uniform(-PI, PI);

@@ -89,7 +89,7 @@ struct gpb_batch {
   DBuf<double> topoD, ctcD, hsD, q, v, tau_in, scratch, stage_q, stage_v, stage_c, hist;
   DBuf<float> topoF, ctcF, hsF;
   DBuf<int32_t> ctcI, laneI, status, queue;
-  DBuf<int64_t> qmap, vmap, cmap;
+  DBuf<int64_t> qmap, vmap, cmap, done;
   DeviceBatch dev() const {
     DeviceBatch b;
     b.npacks = npacks;
@@ -104,6 +104,7 @@ struct gpb_batch {
     b.hsF = hsF.p;
     b.laneI = laneI.p;
     b.status = status.p;
+    b.done = done.p;
     b.q = q.p;
     b.v = v.p;
     b.tau_in = tau_in.p;
@@ -141,6 +142,7 @@ struct gpb_batch {
     qmap.free();
     vmap.free();
     cmap.free();
+    done.free();
   }
 };
 
@@ -457,6 +459,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
   chk(B->hsF.alloc(HF.size()));
   chk(B->laneI.alloc(LI.size()));
   chk(B->status.alloc(npacks * L));
+  chk(B->done.alloc(npacks * L));
   chk(B->q.alloc(rq * L));
   chk(B->v.alloc(rv * L));
   chk(B->tau_in.alloc(rv * L));
@@ -491,6 +494,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
   if (B->v.n) chk(cudaMemsetAsync(B->v.p, 0, B->v.n * sizeof(double), s));
   if (B->tau_in.n) chk(cudaMemsetAsync(B->tau_in.p, 0, B->tau_in.n * sizeof(double), s));
   if (B->status.n) chk(cudaMemsetAsync(B->status.p, 0, B->status.n * sizeof(int32_t), s));
+  if (B->done.n) chk(cudaMemsetAsync(B->done.p, 0, B->done.n * sizeof(int64_t), s));
   chk(cudaStreamSynchronize(s));  // host vectors go out of scope
   if (e != cudaSuccess) {
     B->release();
@@ -699,6 +703,18 @@ extern "C" int gpb_batch_status(gpb_batch* b, int32_t* status) {
                              cudaMemcpyDeviceToHost, b->ctx->stream));
   CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
   for (int64_t i = 0; i < b->n; ++i) status[i] = slots[b->status_slot[i]];
+  return GPB_OK;
+}
+
+extern "C" int gpb_batch_steps_done(gpb_batch* b, int64_t* steps) {
+  if (!b || !steps) return fail(GPB_E_INVAL, "gpb_batch_steps_done: NULL argument");
+  CUDA_TRY(cudaSetDevice(b->ctx->device));
+  std::vector<int64_t> slots(b->done.n);
+  if (!slots.empty())
+    CUDA_TRY(cudaMemcpyAsync(slots.data(), b->done.p, slots.size() * sizeof(int64_t),
+                             cudaMemcpyDeviceToHost, b->ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  for (int64_t i = 0; i < b->n; ++i) steps[i] = slots[b->status_slot[i]];
   return GPB_OK;
 }
 

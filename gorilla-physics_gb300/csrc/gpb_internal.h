@@ -84,7 +84,8 @@ struct DeviceBatch {
   const double* hsD;
   const float* hsF;
   const int32_t* laneI;
-  int32_t* status;         // one int per lane row slot
+  int32_t* status;         // one int per lane slot (pack * LANES + lane)
+  int64_t* done;           // steps completed in the last simulate launch, per slot
   double* q;
   double* v;
   double* tau_in;          // host torques or PD targets (pack layout)

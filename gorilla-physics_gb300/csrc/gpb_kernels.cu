@@ -630,6 +630,7 @@ __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams
     Col<double> tin = col_at(b.tau_in, pd.v, lane);
     Col<double> tau{&c.d(c.L.tau)};
     const bool small = c.nv <= 12;
+    int64_t done = 0;  // steps this instance completed in this launch
     for (int64_t s = 0; s < p.K; ++s) {
       if (*status) break;
       const int64_t sidx = p.step0 + s;
@@ -646,6 +647,7 @@ __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams
       }
       for (int i = 0; i < c.nq; ++i)
         if (!isfinite(q[i])) *status |= 1;
+      done = s + 1;
       if (p.history && p.record_every > 0 && (s + 1) % p.record_every == 0) {
         double* row = p.history + ((s + 1) / p.record_every - 1) * (b.nq_total + b.nv_total);
         const int64_t* qm = b.qmap + pd.q * LANES + lane;
@@ -654,6 +656,7 @@ __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams
         for (int i = 0; i < c.nv; ++i) row[b.nq_total + vm[(size_t)i * LANES]] = v[i];
       }
     }
+    b.done[(int64_t)pk * LANES + lane] = done;
   }
   (void)warps_per_block;
 }

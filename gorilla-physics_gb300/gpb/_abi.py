@@ -77,6 +77,7 @@ SIGNATURES = [
     ("gpb_simulate_steps", C.c_int64, [C.c_double, C.c_double]),
     ("gpb_batch_status", C.c_int, [C.c_void_p, P_i32]),
     ("gpb_batch_clear_status", C.c_int, [C.c_void_p]),
+    ("gpb_batch_steps_done", C.c_int, [C.c_void_p, P_i64]),
     ("gpb_synchronize", C.c_int, [C.c_void_p]),
     ("gpb_batch_set_mapping", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_launch_count", C.c_int64, [C.c_void_p]),

@@ -9,6 +9,7 @@ the C ABI; there is no CPU path.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from typing import Sequence
 
 import numpy as np
@@ -37,9 +38,13 @@ class Context:
         _abi.check(L.gpb_create(device, C.byref(h)), "gpb_create")
         self.h = h
         self.device = device
+        self._batches = weakref.WeakSet()
 
     def close(self) -> None:
+        """Destroys every batch still alive on this context, then the context."""
         if self.h:
+            for b in list(self._batches):
+                b.close()
             _abi.lib().gpb_destroy(self.h)
             self.h = None
 
@@ -73,10 +78,13 @@ class Batch:
             self.model = Model.from_mechanisms(mechanisms)
             init = mechanisms
         L = _abi.lib()
+        if not self.ctx.h:
+            raise ValueError("the context is closed")
         h = C.c_void_p()
         _abi.check(L.gpb_batch_create(self.ctx.h, C.byref(self.model.struct()), C.byref(h)),
                    "gpb_batch_create")
         self.h = h
+        self.ctx._batches.add(self)
         n = self.model.n
         self.q_offset = np.zeros(n + 1, np.int64)
         self.v_offset = np.zeros(n + 1, np.int64)
@@ -96,7 +104,8 @@ class Batch:
 
     def close(self) -> None:
         if getattr(self, "h", None):
-            _abi.lib().gpb_batch_destroy(self.h)
+            if self.ctx.h:  # a closed context already destroyed this batch
+                _abi.lib().gpb_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -131,6 +140,12 @@ class Batch:
     def status(self) -> np.ndarray:
         s = np.zeros(max(self.n, 1), np.int32)
         _abi.check(_abi.lib().gpb_batch_status(self.h, _p(s, _abi.P_i32)), "gpb_batch_status")
+        return s[:self.n]
+
+    def steps_done(self) -> np.ndarray:
+        """Steps each instance completed in the last simulate/step call."""
+        s = np.zeros(max(self.n, 1), np.int64)
+        _abi.check(_abi.lib().gpb_batch_steps_done(self.h, _p(s, _abi.P_i64)), "gpb_batch_steps_done")
         return s[:self.n]
 
     def clear_status(self) -> None:

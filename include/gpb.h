@@ -221,6 +221,9 @@ int64_t gpb_simulate_steps(double final_time, double dt);
 int gpb_batch_status(gpb_batch* batch, int32_t* status);
 /* Clears all status words (e.g. after the caller repaired the state). */
 int gpb_batch_clear_status(gpb_batch* batch);
+/* Steps each instance completed in the last gpb_simulate / gpb_step call
+ * (fewer than K for an instance frozen by a status bit), n_instances int64. */
+int gpb_batch_steps_done(gpb_batch* batch, int64_t* steps);
 
 /* Waits for all work of the context's stream. */
 int gpb_synchronize(gpb_ctx* ctx);

@@ -82,12 +82,20 @@ def dims(model, i):
     return nq.value, nv.value, nc.value
 
 
+def _checked(model, i, q, v, tau=None):
+    nq, nv, nc = dims(model, i)
+    q = np.ascontiguousarray(q, float).ravel()
+    v = np.ascontiguousarray(v, float).ravel()
+    t = None if tau is None else np.ascontiguousarray(tau, float).ravel()
+    if q.size != nq or v.size != nv or (t is not None and t.size != nv):
+        raise ValueError(f"instance {i}: expected {nq} q / {nv} v values, got {q.size} / {v.size}"
+                         + ("" if t is None else f" / tau {t.size}"))
+    return nq, nv, nc, q, v, t
+
+
 def dynamics(model, i, q, v, tau=None, solver=LU, contact_forces=False):
     """q̈ (and contact forces) of instance i; returns (qdd, status[, cforce])."""
-    nq, nv, nc = dims(model, i)
-    q = np.ascontiguousarray(q, float)
-    v = np.ascontiguousarray(v, float)
-    t = None if tau is None else np.ascontiguousarray(tau, float)
+    nq, nv, nc, q, v, t = _checked(model, i, q, v, tau)
     qdd = np.zeros(max(nv, 1))
     cf = np.zeros(max(3 * nc, 1))
     st = lib().oracle_dynamics(_m(model), i, _p(q), _p(v), _p(t), solver, _p(qdd), _p(cf))
@@ -111,9 +119,8 @@ def energy(model, i, q, v):
 
 
 def step(model, i, q, v, dt, tau=None, integrator=0, solver=LU):
-    q = np.array(q, float)
-    v = np.array(v, float)
-    t = None if tau is None else np.ascontiguousarray(tau, float)
+    _, _, _, q, v, t = _checked(model, i, q, v, tau)
+    q, v = q.copy(), v.copy()
     st = lib().oracle_step(_m(model), i, _p(q), _p(v), _p(t), dt, integrator, solver)
     return q, v, st
 
@@ -128,10 +135,8 @@ CONTROL = {"host": 0, "open_loop": 1, "pd": 2}
 def simulate(model, i, q, v, dt, K, integrator=0, solver=LU, control="host", ctl=None, seed=0,
              resample_every=10, sigma=1.0, kp=0.0, kd=0.0, step0=0, record_every=0):
     """K steps of instance i; returns (q, v, status, history)."""
-    nq, nv, _ = dims(model, i)
-    q = np.array(q, float)
-    v = np.array(v, float)
-    c = None if ctl is None else np.ascontiguousarray(ctl, float)
+    nq, nv, _, q, v, c = _checked(model, i, q, v, ctl)
+    q, v = q.copy(), v.copy()
     hist = np.zeros(max((K // record_every) * (nq + nv), 1)) if record_every > 0 else None
     st = lib().oracle_simulate(_m(model), i, _p(q), _p(v), dt, K, step0, integrator, solver,
                                CONTROL[control], seed, resample_every, sigma, kp, kd, _p(c),

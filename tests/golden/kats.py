@@ -201,6 +201,6 @@ def dynamics_cases():
     base_ang = -1.0 / 0.4
     base_lin_x = -1.0 / 1.0 / 1.0
     exp = [0, 0, base_ang, base_lin_x, 0, -G, -base_ang + 1.0 / 1.0 + -base_lin_x * 1.0]
-    cases.append(("motor_turning_mass", mt, [0, 0, 0, 1, 0, 0, 0], [0.0] * 7, [0.0] * 6 + [1.0],
+    cases.append(("motor_turning_mass", mt, [0, 0, 0, 1, 0, 0, 0, 0.0], [0.0] * 7, [0.0] * 6 + [1.0],
                   exp, 1e-5, "src/dynamics.rs:1194-1251"))
     return cases
