@@ -83,6 +83,7 @@ struct gpb_batch {
   int64_t nq_total = 0, nv_total = 0, nc_total = 0;
   std::vector<PackDesc> packs_h;
   int64_t q_slots = 0, v_slots = 0, c_slots = 0;
+  int64_t scratch_words = 0;  // 8-byte words of per-instance scratch, all packs
   std::vector<int32_t> status_slot;  // user instance -> status slot (pack*32+lane)
   DBuf<PackDesc> packs;
   DBuf<uint32_t> topoW;
@@ -445,6 +446,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
   auto chk = [&](cudaError_t x) {
     if (x != cudaSuccess && e == cudaSuccess) e = x;
   };
+  B->scratch_words = rs * L;
   B->q_slots = rq * L;
   B->v_slots = rv * L;
   B->c_slots = rc * 3 * L;
@@ -723,6 +725,26 @@ extern "C" int gpb_batch_clear_status(gpb_batch* b) {
   CUDA_TRY(cudaSetDevice(b->ctx->device));
   if (b->status.n) CUDA_TRY(cudaMemsetAsync(b->status.p, 0, b->status.n * sizeof(int32_t), b->ctx->stream));
   CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return GPB_OK;
+}
+
+// q̈ from caller device buffers with the library's static scratch: no device
+// memory is allocated or freed here (see gpb.h).
+extern "C" int gpb_dynamics_static(gpb_batch* b, const double* q, const double* v,
+                                   const double* tau, int precision, double* qdd, void* stream) {
+  if (!b || !q || !v || !qdd) return fail(GPB_E_INVAL, "gpb_dynamics_static: NULL argument");
+  if (int r = check_enums(0, precision)) return r;
+  const int64_t limit = (int64_t)(GPB_STATIC_SCRATCH_BYTES / sizeof(double));
+  if (b->scratch_words > limit)
+    return fail(GPB_E_RANGE, "gpb_dynamics_static: the batch needs " +
+                                 std::to_string(b->scratch_words * 8) + " bytes of scratch; the static array holds " +
+                                 std::to_string((int64_t)GPB_STATIC_SCRATCH_BYTES) +
+                                 " (use gpb_dynamics, or a smaller batch)");
+  CUDA_TRY(cudaSetDevice(b->ctx->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : b->ctx->stream;
+  CUDA_TRY(launch_dynamics_static(b->dev(), b->ctx->device, b->scratch_words, precision, q, v, tau,
+                                  qdd, s));
+  b->ctx->launches++;
   return GPB_OK;
 }
 

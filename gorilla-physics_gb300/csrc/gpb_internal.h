@@ -122,6 +122,11 @@ cudaError_t launch_scatter(const int64_t* map, int64_t slots, const double* src,
                            cudaStream_t s);
 cudaError_t launch_gather(const int64_t* map, int64_t slots, const double* src, double* dst,
                           cudaStream_t s);
+// gpb_dynamics_static: the dynamics kernel with its scratch in the library's
+// static device array (cudaErrorInvalidValue if scratch_words exceeds it).
+cudaError_t launch_dynamics_static(const DeviceBatch& b, int device, int64_t scratch_words,
+                                   int precision, const double* q, const double* v,
+                                   const double* tau, double* qdd, cudaStream_t s);
 
 // Open-loop torque draw shared bit for bit by host and device.
 __host__ __device__ double open_loop_tau(uint32_t seed, int64_t inst, int64_t block, int32_t dof,

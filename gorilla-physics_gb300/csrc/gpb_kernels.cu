@@ -17,6 +17,10 @@
 #include <math.h>
 #include <string.h>
 
+#include <mutex>
+
+#include "gpb.h"
+
 #include "gpb_device.cuh"
 #include "gpb_internal.h"
 #include "gpb_rng.h"
@@ -752,6 +756,94 @@ cudaError_t launch_gather(const int64_t* map, int64_t slots, const double* src, 
   int64_t blocks = (slots + 255) / 256;
   if (blocks > 65535) blocks = 65535;
   gather_kernel<<<(unsigned)blocks, 256, 0, s>>>(map, slots, src, dst);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Dynamics without any device allocation.
+//
+// Some callers cannot allocate device memory when they evaluate the dynamics:
+// a control loop with a hard real-time budget, or a host application that hands
+// the GPU out through its own memory pool and forbids cudaMalloc after start-up.
+// For them the per-instance working memory of one dynamics evaluation (spatial
+// quantities, the mass matrix and its factor) lives in the fixed array below
+// instead of the batch's scratch buffer.  The array is part of the library
+// image: every GPU that loads the library holds GPB_STATIC_SCRATCH_BYTES until
+// the process exits.  All calls share it, so calls whose kernels overlap on the
+// GPU (on different streams, or from different host threads) race and must be
+// ordered by the caller.  The kernel writes every scratch word before it reads
+// it (tree-shaped mechanisms clear their mass-matrix triangle in the kernel), so
+// nothing is left over from the previous call's contents.
+
+static __device__ __align__(256) double gpb_static_scratch[GPB_STATIC_SCRATCH_BYTES / sizeof(double)];
+
+// Host-side stand-in of the array above is not a device address: the address a
+// kernel may use is looked up once per device, with that device current.
+constexpr int kMaxDevices = 64;
+static std::mutex g_static_mu;
+static double* g_static_ptr[kMaxDevices] = {};
+
+static cudaError_t static_scratch_address(int device, double** out) {
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_ptr[device]) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return e;
+    double* p = nullptr;
+    e = cudaGetSymbolAddress((void**)&p, gpb_static_scratch);
+    if (e != cudaSuccess) return e;
+    g_static_ptr[device] = p;
+  }
+  *out = g_static_ptr[device];
+  return cudaSuccess;
+}
+
+// The dynamics kernel with user-order state read from caller buffers into the
+// static scratch (the q / v / τ slots of each instance's scratch layout).
+template <typename R>
+__global__ void __launch_bounds__(128)
+    dynamics_static_kernel(DeviceBatch b, int precision, const double* qu, const double* vu,
+                           const double* tu, double* qddu) {
+  const int lane = threadIdx.x & 31;
+  const int pk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (pk >= b.npacks) return;
+  const PackDesc pd = b.packs[pk];
+  if (lane >= pd.count) return;
+  LaneCtx<R> c = make_ctx<R>(b, pd, lane);
+  Col<double> q{&c.d(c.L.qs)}, v{&c.d(c.L.vs)}, tau{&c.d(c.L.tau)}, qdd{&c.d(c.L.facc)};
+  const int64_t* qm = b.qmap + pd.q * LANES + lane;
+  const int64_t* vm = b.vmap + pd.v * LANES + lane;
+  for (int i = 0; i < c.nq; ++i) q[i] = qu[qm[(size_t)i * LANES]];
+  for (int i = 0; i < c.nv; ++i) {
+    v[i] = vu[vm[(size_t)i * LANES]];
+    tau[i] = tu ? tu[vm[(size_t)i * LANES]] : 0.0;
+  }
+  Col<double> none{nullptr};
+  int st;
+  if (precision == 1 && c.nv <= 12)
+    st = lane_dynamics<R, float>(c, q, v, tau, true, qdd, none, false);
+  else
+    st = lane_dynamics<R, double>(c, q, v, tau, true, qdd, none, false);
+  b.status[(int64_t)pk * LANES + lane] |= st;
+  for (int i = 0; i < c.nv; ++i) qddu[vm[(size_t)i * LANES]] = qdd[i];
+}
+
+cudaError_t launch_dynamics_static(const DeviceBatch& batch, int device, int64_t scratch_words,
+                                   int precision, const double* q, const double* v,
+                                   const double* tau, double* qdd, cudaStream_t s) {
+  if (scratch_words > (int64_t)(GPB_STATIC_SCRATCH_BYTES / sizeof(double))) return cudaErrorInvalidValue;
+  double* base = nullptr;
+  cudaError_t e = static_scratch_address(device, &base);
+  if (e != cudaSuccess) return e;
+  DeviceBatch b = batch;
+  b.scratch = base;
+  const int threads = 128;
+  unsigned grid = (unsigned)((b.npacks + 3) / 4);
+  if (grid == 0) return cudaSuccess;
+  if (precision == 1)
+    dynamics_static_kernel<float><<<grid, threads, 0, s>>>(b, precision, q, v, tau, qdd);
+  else
+    dynamics_static_kernel<double><<<grid, threads, 0, s>>>(b, precision, q, v, tau, qdd);
   return cudaGetLastError();
 }
 

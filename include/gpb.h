@@ -183,6 +183,31 @@ int gpb_dynamics(gpb_batch* batch, const double* tau, int precision, double* qdd
                  double* contact_force);
 
 /*
+ * gpb_dynamics_static — no counterpart in the reference.
+ *
+ * The same q̈ as gpb_dynamics, for callers that cannot allocate device memory
+ * when they evaluate the dynamics (a hard real-time control loop, or a host
+ * that owns the GPU through its own memory pool and forbids cudaMalloc once
+ * running).  Nothing is allocated or freed: q (nq_total), v (nv_total), tau
+ * (nv_total, or NULL for zero torque) and qdd (nv_total) are the caller's
+ * DEVICE buffers in the flattened user order, and the kernel's working memory
+ * is a fixed array of GPB_STATIC_SCRATCH_BYTES compiled into the library — each
+ * GPU that loads the library holds it until the process exits.  A batch whose
+ * scratch needs more (about 32 KB per instance of a 48-DOF chain, 1 KB for an
+ * acrobot) is rejected with GPB_E_RANGE.
+ *
+ * The kernel runs asynchronously on `stream` (a cudaStream_t; NULL = the
+ * batch's context stream); read qdd after synchronising that stream.  The first
+ * call on a device looks up the array's device address, so make that first call
+ * before any stream capture.  All calls share the one array: calls whose
+ * kernels overlap on the GPU race, so order them on one stream.  No state is
+ * carried from one call to the next.
+ */
+#define GPB_STATIC_SCRATCH_BYTES (16u << 20)
+int gpb_dynamics_static(gpb_batch* batch, const double* q, const double* v, const double* tau,
+                        int precision, double* qdd, void* stream);
+
+/*
  * step (src/simulate.rs:20-83) for every instance: one integrator step of
  * size dt with joint torques `tau` (NULL = zero).  State stays on the device.
  */
