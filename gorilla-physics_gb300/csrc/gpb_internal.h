@@ -57,9 +57,10 @@ __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, 
   s.S = o; o += 6 * nv;
   s.I = o; o += 10 * nb;
   s.F = o; o += 6 * nb;
-  s.M = o; o += nv * (nv + 1) / 2;
-  s.D = o; o += nv;
-  s.rhs = o; o += nv;
+  const int nT = (nv + 3) / 4;  // mass matrix in 4x4 tiles, n padded to 4 nT
+  s.M = o; o += nT * (nT + 1) / 2 * 16;
+  s.D = o; o += 4 * nT;
+  s.rhs = o; o += 4 * nT;
   s.q0 = o; o += nq;
   s.v0 = o; o += nv;
   s.qs = o; o += nq;

@@ -173,6 +173,171 @@ __device__ __forceinline__ V3<R> contact_force(int model, R z, V3<R> n, V3<R> ve
   return f;
 }
 
+// Offset of H(i, j), i ≥ j, in the tile-major packed lower triangle: 4×4 tiles
+// (I, J), I ≥ J, stored one after another (16 words each, row-major inside).
+__device__ __forceinline__ int tix(int i, int j) {
+  const int I = i >> 2, J = j >> 2;
+  return (((I * (I + 1)) >> 1) + J) * 16 + ((i & 3) << 2) + (j & 3);
+}
+__device__ __forceinline__ int tile(int I, int J) { return (((I * (I + 1)) >> 1) + J) * 16; }
+
+// a·b of two spatial vectors with two independent partial sums.
+template <typename R>
+__device__ __forceinline__ R sdot2(const SV<R>& a, const SV<R>& b) {
+  return (a.w.x * b.w.x + a.w.y * b.w.y + a.w.z * b.w.z) + (a.v.x * b.v.x + a.v.y * b.v.y + a.v.z * b.v.z);
+}
+
+// Cholesky H = L Lᵀ (left-looking, 4×4 register tiles: every tile update is 16
+// independent multiply-add chains over 32 loaded words — 2 FMAs per load) and
+// the solves L y = rhs, Lᵀ x = y.  n is padded to a multiple of 4 with identity
+// rows.  Writes q̈ into `qdd`; returns GPB status bits.
+template <typename R, typename RC>
+__device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& c, Col<double> qdd) {
+  const int nv = c.nv, nT = (nv + 3) >> 2, np = nT << 2;
+  const int M = c.L.M;
+  for (int i = nv; i < np; ++i) {
+    for (int j = 0; j < i; ++j) c.d(M + tix(i, j)) = 0.0;
+    c.d(M + tix(i, i)) = 1.0;
+    c.d(c.L.rhs + i) = 0.0;
+  }
+  int st = 0;
+  for (int J = 0; J < nT; ++J) {
+    const int tJJ = M + tile(J, J);
+    RC a[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int s = 0; s <= r; ++s) a[r][s] = RC(c.d(tJJ + 4 * r + s));
+    for (int K = 0; K < J; ++K) {
+      const int tJK = M + tile(J, K);
+      RC l[4][4];
+#pragma unroll
+      for (int e = 0; e < 16; ++e) l[e >> 2][e & 3] = RC(c.d(tJK + e));
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int s = 0; s <= r; ++s)
+          a[r][s] -= (l[r][0] * l[s][0] + l[r][1] * l[s][1]) + (l[r][2] * l[s][2] + l[r][3] * l[s][3]);
+    }
+    RC inv[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+#pragma unroll
+      for (int s = 0; s <= r; ++s) {
+        RC x = a[r][s];
+#pragma unroll
+        for (int m = 0; m < s; ++m) x -= a[r][m] * a[s][m];
+        if (r == s) {
+          if (!(x > RC(0))) {
+            st |= 2;  // GPB_ST_CHOL_FAIL
+            x = RC(1);
+          }
+          a[r][r] = sqrt(x);
+          inv[r] = RC(1) / a[r][r];
+        } else {
+          a[r][s] = x * inv[s];
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+#pragma unroll
+      for (int s = 0; s <= r; ++s) c.d(tJJ + 4 * r + s) = double(a[r][s]);
+      c.d(c.L.D + 4 * J + r) = double(inv[r]);
+    }
+    for (int I = J + 1; I < nT; ++I) {
+      const int tIJ = M + tile(I, J);
+      RC b[4][4];
+#pragma unroll
+      for (int e = 0; e < 16; ++e) b[e >> 2][e & 3] = RC(c.d(tIJ + e));
+      for (int K = 0; K < J; ++K) {
+        const int tIK = M + tile(I, K), tJK = M + tile(J, K);
+        RC x[4][4], y[4][4];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          x[e >> 2][e & 3] = RC(c.d(tIK + e));
+          y[e >> 2][e & 3] = RC(c.d(tJK + e));
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int s = 0; s < 4; ++s)
+            b[r][s] -= (x[r][0] * y[s][0] + x[r][1] * y[s][1]) + (x[r][2] * y[s][2] + x[r][3] * y[s][3]);
+      }
+      // b ← b L_JJ⁻ᵀ
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          RC x = b[r][s];
+#pragma unroll
+          for (int m = 0; m < s; ++m) x -= b[r][m] * a[s][m];
+          b[r][s] = x * inv[s];
+        }
+#pragma unroll
+      for (int e = 0; e < 16; ++e) c.d(tIJ + e) = double(b[e >> 2][e & 3]);
+    }
+  }
+  // forward substitution L y = rhs
+  for (int I = 0; I < nT; ++I) {
+    RC y[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) y[r] = RC(c.d(c.L.rhs + 4 * I + r));
+    for (int K = 0; K < I; ++K) {
+      const int tIK = M + tile(I, K);
+      RC z[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) z[m] = RC(c.d(c.L.rhs + 4 * K + m));
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        y[r] -= (RC(c.d(tIK + 4 * r)) * z[0] + RC(c.d(tIK + 4 * r + 1)) * z[1]) +
+                (RC(c.d(tIK + 4 * r + 2)) * z[2] + RC(c.d(tIK + 4 * r + 3)) * z[3]);
+    }
+    const int tII = M + tile(I, I);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      RC x = y[r];
+#pragma unroll
+      for (int m = 0; m < r; ++m) x -= RC(c.d(tII + 4 * r + m)) * y[m];
+      y[r] = x * RC(c.d(c.L.D + 4 * I + r));
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) c.d(c.L.rhs + 4 * I + r) = double(y[r]);
+  }
+  // back substitution Lᵀ x = y
+  for (int I = nT - 1; I >= 0; --I) {
+    RC x[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) x[r] = RC(c.d(c.L.rhs + 4 * I + r));
+    for (int K = I + 1; K < nT; ++K) {
+      const int tKI = M + tile(K, I);
+      RC z[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) z[m] = RC(c.d(c.L.rhs + 4 * K + m));
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        x[r] -= (RC(c.d(tKI + r)) * z[0] + RC(c.d(tKI + 4 + r)) * z[1]) +
+                (RC(c.d(tKI + 8 + r)) * z[2] + RC(c.d(tKI + 12 + r)) * z[3]);
+    }
+    const int tII = M + tile(I, I);
+#pragma unroll
+    for (int r = 3; r >= 0; --r) {
+      RC v = x[r];
+#pragma unroll
+      for (int m = r + 1; m < 4; ++m) v -= RC(c.d(tII + 4 * m + r)) * x[m];
+      x[r] = v * RC(c.d(c.L.D + 4 * I + r));
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) c.d(c.L.rhs + 4 * I + r) = double(x[r]);
+  }
+  for (int i = 0; i < nv; ++i) {
+    const double x = c.d(c.L.rhs + i);
+    qdd[i] = x;
+    if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
+  }
+  return st;
+}
+
 // One dynamics evaluation (src/dynamics.rs:322-364): reads q, v, tau (double
 // columns), writes q̈ into `qdd`.  Returns GPB status bits.
 template <typename R, typename RC>
@@ -359,8 +524,9 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
   const int nv = c.nv;
   if (!c.chain) {
     // Non-ancestor pairs are not written by the fill but hold Cholesky fill-in
-    // from the previous evaluation: clear the packed triangle first.
-    const int nm = nv * (nv + 1) / 2;
+    // from the previous evaluation: clear the tiled triangle first.
+    const int nT = (nv + 3) >> 2;
+    const int nm = (nT * (nT + 1) >> 1) * 16;
     for (int e = 0; e < nm; ++e) c.d(c.L.M + e) = 0.0;
   }
   SI<R> cI;
@@ -387,11 +553,10 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
       c.d(c.L.rhs + vo + k) = rhs - double(sdot(Sk, f));
       SV<R> Fk = imul(Ic, Sk);
       // row vo+k of H: F_kᵀ S_l for every column l of this joint and its ancestors
-      int row = vo + k;
-      int rowbase = c.L.M + row * (row + 1) / 2;
+      const int row = vo + k;
       for (int l = 0; l <= k; ++l) {
         SV<R> Sl = l == k ? Sk : load_sv(c, c.L.S + 6 * (vo + l));
-        c.d(rowbase + vo + l) = double(sdot(Fk, Sl));
+        c.d(c.L.M + tix(row, vo + l)) = double(sdot2(Fk, Sl));
       }
       int a = parent;
       while (a != 0) {
@@ -400,7 +565,7 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
         int nva = ta == 3 ? 6 : (ta == 0 ? 0 : 1);
         for (int l = 0; l < nva; ++l) {
           SV<R> Sl = load_sv(c, c.L.S + 6 * (voa + l));
-          c.d(rowbase + voa + l) = double(sdot(Fk, Sl));
+          c.d(c.L.M + tix(row, voa + l)) = double(sdot2(Fk, Sl));
         }
         a = (wa >> 4) & 255;
       }
@@ -424,44 +589,7 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
     }
   }
 
-  // ---- Cholesky (row by row) and the two triangular solves -------------
-  // M holds H in packed lower storage; entries of non-ancestor pairs were
-  // zeroed before the call (trees) or are all written (chains).
-  int st = 0;
-  for (int i = 0; i < nv; ++i) {
-    int ri = c.L.M + i * (i + 1) / 2;
-    for (int j = 0; j <= i; ++j) {
-      int rj = c.L.M + j * (j + 1) / 2;
-      RC s = RC(c.d(ri + j));
-      for (int k = 0; k < j; ++k) s -= RC(c.d(ri + k)) * RC(c.d(rj + k));
-      if (i == j) {
-        if (!(s > RC(0))) {
-          st |= 2;  // GPB_ST_CHOL_FAIL
-          s = RC(1);
-        }
-        RC l = sqrt(s);
-        c.d(ri + i) = double(l);
-        c.d(c.L.D + i) = double(RC(1) / l);
-      } else {
-        c.d(ri + j) = double(s * RC(c.d(c.L.D + j)));
-      }
-    }
-  }
-  for (int i = 0; i < nv; ++i) {
-    int ri = c.L.M + i * (i + 1) / 2;
-    RC s = RC(c.d(c.L.rhs + i));
-    for (int k = 0; k < i; ++k) s -= RC(c.d(ri + k)) * RC(c.d(c.L.rhs + k));
-    c.d(c.L.rhs + i) = double(s * RC(c.d(c.L.D + i)));
-  }
-  for (int i = nv - 1; i >= 0; --i) {
-    RC s = RC(c.d(c.L.rhs + i));
-    for (int k = i + 1; k < nv; ++k) s -= RC(c.d(c.L.M + k * (k + 1) / 2 + i)) * RC(c.d(c.L.rhs + k));
-    double x = double(s * RC(c.d(c.L.D + i)));
-    c.d(c.L.rhs + i) = x;
-    qdd[i] = x;
-    if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
-  }
-  return st;
+  return lane_cholesky_solve<R, RC>(c, qdd);
 }
 
 // quaternion_derivative (src/util.rs:83-102) and the pose update of
