@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--instances", type=int, default=65536)
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
-    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"])
+    ap.add_argument("--precision", default="all", choices=["all", "fp64", "mixed", "refined"])
     return ap.parse_args()
 
 
@@ -254,9 +254,11 @@ def run_gpu(args):
     inst_flops = model_flops(M, 0).astype(np.float64)
 
     results = {}
-    precs = {"both": ["fp64", "mixed"], "mixed": ["mixed"], "fp64": ["fp64"]}[args.precision]
+    precs = {"all": ["fp64", "mixed", "refined"], "fp64": ["fp64"], "mixed": ["mixed"],
+             "refined": ["refined"]}[args.precision]
+    PREC = {"fp64": gpb.FP64, "mixed": gpb.MIXED, "refined": gpb.MIXED_REFINED}
     for name in precs:
-        prec = gpb.FP64 if name == "fp64" else gpb.MIXED
+        prec = PREC[name]
         B.update(q0, v0)
         B.clear_status()
         if args.warmup:
@@ -280,18 +282,29 @@ def run_gpu(args):
                          "failed_instances": bad, "launches": timed_launches,
                          "done": reduce_sum(float(done.sum())),
                          "flops": reduce_sum(float(np.dot(done, inst_flops)))}
-    # q̈ error of mixed against FP64 at the final state
-    err = None
-    if len(precs) == 2:
-        err = {"final": qdd_error(B, gpb, gpb.MIXED, f"after the {args.steps}-step timed run")}
-        B.update(q0, v0)
-        B.clear_status()
-        err["initial"] = qdd_error(B, gpb, gpb.MIXED, "the configuration's initial states")
+    # q̈ error of the reduced-precision modes against FP64, at the final state of
+    # the last timed run and at the configuration's initial states
+    errs = {}
+    for name in [p for p in precs if p != "fp64"]:
+        errs[name] = {"final": qdd_error(B, gpb, PREC[name], f"after the {args.steps}-step "
+                                                             f"timed run ({precs[-1]})")}
+    B.update(q0, v0)
+    B.clear_status()
+    for name in errs:
+        errs[name]["initial"] = qdd_error(B, gpb, PREC[name], "the configuration's initial states")
+    # headline: the fastest mode that meets the stated bound (≤ 1e-5 on ≥ 99 % of
+    # instances at both states), else FP64
+    head_name = "fp64" if "fp64" in results else precs[0]
+    for name in ["mixed", "refined"]:
+        e = errs.get(name)
+        if name in results and e and all(x["frac_le_1e-5"] >= 0.99 for x in e.values()):
+            if results[name]["kernel_ms"] < results[head_name]["kernel_ms"]:
+                head_name = name
     # e2e through the public API: host (pinned) state in, K steps, state out
     q_h = torch.from_numpy(q0).pin_memory()
     v_h = torch.from_numpy(v0).pin_memory()
     qn, vn = q_h.numpy(), v_h.numpy()
-    prec = gpb.MIXED if "mixed" in precs else gpb.FP64
+    prec = PREC[head_name]
     barrier()
     ctx.synchronize()
     t0 = time.perf_counter()
@@ -302,7 +315,7 @@ def run_gpu(args):
     e2e_s = reduce_max(e2e_s)
     e2e_done = reduce_sum(float(B.steps_done().sum()))
 
-    head = results["mixed" if "mixed" in results else "fp64"]
+    head = results[head_name]
     value = head["done"] / (head["kernel_ms"] * 1e-3)
 
     def peak(precision):
@@ -323,23 +336,29 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["kernel_ms"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64" if "mixed" in results else "f64",
+        "dtype": {"fp64": "f64", "mixed": "f32 sweeps + f64 Cholesky (n>12) + f64 state",
+                  "refined": "f32 solve + f64 residual refinement + f64 state"}[head_name],
         "data": "synthetic (seeded Philox4x32-10 draws of the configuration's distributions)",
         "config": {"workload": f"{CONFIG_NAME[args.config]} x {args.instances} per GPU",
+                   "precision_mode": head_name,
                    "dof": "U{2..48}" if args.config == 1 else None, "dt": dt,
                    "integrator": "semi-implicit Euler", "control": CONTROL[args.config],
                    "l2": "inputs larger than L2 (topology + state + scratch > 129 MB)"},
         "gpu_launches": head["launches"],
     }
+    bound = {"fp64": ("fp64", p64), "mixed": ("fp32", p32), "refined": ("fp32", p32)}
+    line["modes"] = {}
+    for name, r in results.items():
+        line["modes"][name] = {
+            "value": r["done"] / (r["kernel_ms"] * 1e-3), "ms_per_step": r["kernel_ms"] / args.steps,
+            "roofline": roof(r, *bound[name]),
+            "qdd_rel_err_vs_fp64": errs.get(name)}
     if "fp64" in results:
-        line["fp64"] = {"value": results["fp64"]["done"] / (results["fp64"]["kernel_ms"] * 1e-3),
-                        "ms_per_step": results["fp64"]["kernel_ms"] / args.steps,
-                        "roofline": roof(results["fp64"], "fp64", p64)}
-    if "mixed" in results and "fp64" in results:
-        line["mixed_over_fp64"] = line["value"] / line["fp64"]["value"]
-        line["qdd_rel_err_mixed_vs_fp64"] = err
-    line["roofline"] = roof(head, "fp32" if "mixed" in results else "fp64",
-                            p32 if "mixed" in results else p64)
+        line["fp64"] = line["modes"]["fp64"]
+        for name in ("mixed", "refined"):
+            if name in results:
+                line[f"{name}_over_fp64"] = line["modes"][name]["value"] / line["fp64"]["value"]
+    line["roofline"] = roof(head, *bound[head_name])
     line["peaks_measured"] = {"fp64_tflops": p64, "fp32_tflops": p32}
     line["clocks"] = head["clocks"]
     line["failed_instances"] = {k: r["failed_instances"] for k, r in results.items()}

@@ -579,7 +579,8 @@ extern "C" int gpb_get_state(gpb_batch* b, double* q, double* v) {
 
 static int check_enums(int integrator, int precision) {
   if (integrator < 0 || integrator > 2) return fail(GPB_E_INVAL, "unknown integrator");
-  if (precision != GPB_FP64 && precision != GPB_MIXED) return fail(GPB_E_INVAL, "unknown precision");
+  if (precision != GPB_FP64 && precision != GPB_MIXED && precision != GPB_MIXED_REFINED)
+    return fail(GPB_E_INVAL, "unknown precision");
   return GPB_OK;
 }
 

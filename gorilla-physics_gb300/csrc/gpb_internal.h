@@ -46,7 +46,7 @@ struct PackDesc {
 // Scratch sub-array offsets (rows of 8-byte words; R-typed arrays use the same
 // row pitch so that the float and double kernels share one layout).
 struct ScratchLayout {
-  int32_t X, V, A, S, I, F, M, D, rhs, q0, v0, qs, vs, facc, tau, cf, total;
+  int32_t X, V, A, S, I, F, C, M, D, rhs, q0, v0, qs, vs, facc, tau, cf, total;
 };
 __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, int nc) {
   ScratchLayout s;
@@ -55,8 +55,9 @@ __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, 
   s.V = o; o += 6 * nb;
   s.A = o; o += 6 * nb;
   s.S = o; o += 6 * nv;
-  s.I = o; o += 10 * nb;
+  s.I = o; o += 12 * nb;  // world inertia (10) or, in link coordinates, (Rrel, t) (12)
   s.F = o; o += 6 * nb;
+  s.C = o; o += 10 * nb;  // link coordinates: composite inertia accumulated from branches
   const int nT = (nv + 3) / 4;  // mass matrix in 4x4 tiles, n padded to 4 nT
   s.M = o; o += nT * (nT + 1) / 2 * 16;
   s.D = o; o += 4 * nT;

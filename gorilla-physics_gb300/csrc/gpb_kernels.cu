@@ -18,6 +18,7 @@
 #include <string.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "gpb.h"
 
@@ -74,6 +75,7 @@ struct LaneCtx {
   ScratchLayout L;
   R* sR;              // scratch viewed as R (row pitch = LANES * 8 bytes)
   double* sD;         // scratch viewed as double
+  char* s0;           // scratch row 0, lane 0
   __device__ __forceinline__ uint32_t w(int e) const { return W[(size_t)e * LANES]; }
   __device__ __forceinline__ R t(int e) const { return T[(size_t)e * LANES]; }
   // R-typed scratch element (e in rows of 8-byte words)
@@ -81,6 +83,12 @@ struct LaneCtx {
     return *reinterpret_cast<R*>(reinterpret_cast<char*>(sR) + (size_t)e * LANES * 8);
   }
   __device__ __forceinline__ double& d(int e) const { return sD[(size_t)e * LANES]; }
+  // T-typed scratch element: the factor and right-hand side are kept in the
+  // factorisation's own precision (no conversions on the FP64 pipe)
+  template <typename T>
+  __device__ __forceinline__ T& x(int e) const {
+    return *reinterpret_cast<T*>(s0 + (size_t)e * LANES * 8 + (size_t)lane * sizeof(T));
+  }
 };
 
 template <typename R>
@@ -134,15 +142,18 @@ __device__ __forceinline__ M3<R> quat_to_mat(R x, R y, R z, R w) {
   return m;
 }
 
+// sin / cos of a joint angle held in double, returned in the sweep precision.
 template <typename R>
-__device__ __forceinline__ void sincos_r(R a, R* s, R* c);
+__device__ __forceinline__ void sincos_q(double q, R* s, R* c);
 template <>
-__device__ __forceinline__ void sincos_r<double>(double a, double* s, double* c) {
-  sincos(a, s, c);
+__device__ __forceinline__ void sincos_q<double>(double q, double* s, double* c) {
+  sincos(q, s, c);
 }
 template <>
-__device__ __forceinline__ void sincos_r<float>(float a, float* s, float* c) {
-  sincosf(a, s, c);
+__device__ __forceinline__ void sincos_q<float>(double q, float* s, float* c) {
+  // reduce by 2π in double first: float(q) alone loses ~q·6e-8 rad
+  const double r = fma(-6.283185307179586477, rint(q * 0.15915494309189533577), q);
+  sincosf((float)r, s, c);
 }
 
 // Contact force of one point against one half-space (src/contact.rs:260-338),
@@ -187,6 +198,9 @@ __device__ __forceinline__ R sdot2(const SV<R>& a, const SV<R>& b) {
   return (a.w.x * b.w.x + a.w.y * b.w.y + a.w.z * b.w.z) + (a.v.x * b.v.x + a.v.y * b.v.y + a.v.z * b.v.z);
 }
 
+template <typename R, typename RC>
+__device__ __noinline__ void lane_solve(const LaneCtx<R>& c);
+
 // Cholesky H = L Lᵀ (left-looking, 4×4 register tiles: every tile update is 16
 // independent multiply-add chains over 32 loaded words — 2 FMAs per load) and
 // the solves L y = rhs, Lᵀ x = y.  n is padded to a multiple of 4 with identity
@@ -196,9 +210,9 @@ __device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& c, Col<double>
   const int nv = c.nv, nT = (nv + 3) >> 2, np = nT << 2;
   const int M = c.L.M;
   for (int i = nv; i < np; ++i) {
-    for (int j = 0; j < i; ++j) c.d(M + tix(i, j)) = 0.0;
-    c.d(M + tix(i, i)) = 1.0;
-    c.d(c.L.rhs + i) = 0.0;
+    for (int j = 0; j < i; ++j) c.template x<RC>(M + tix(i, j)) = RC(0);
+    c.template x<RC>(M + tix(i, i)) = RC(1);
+    c.template x<RC>(c.L.rhs + i) = RC(0);
   }
   int st = 0;
   for (int J = 0; J < nT; ++J) {
@@ -207,12 +221,12 @@ __device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& c, Col<double>
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
-      for (int s = 0; s <= r; ++s) a[r][s] = RC(c.d(tJJ + 4 * r + s));
+      for (int s = 0; s <= r; ++s) a[r][s] = (c.template x<RC>(tJJ + 4 * r + s));
     for (int K = 0; K < J; ++K) {
       const int tJK = M + tile(J, K);
       RC l[4][4];
 #pragma unroll
-      for (int e = 0; e < 16; ++e) l[e >> 2][e & 3] = RC(c.d(tJK + e));
+      for (int e = 0; e < 16; ++e) l[e >> 2][e & 3] = (c.template x<RC>(tJK + e));
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -242,21 +256,21 @@ __device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& c, Col<double>
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
 #pragma unroll
-      for (int s = 0; s <= r; ++s) c.d(tJJ + 4 * r + s) = double(a[r][s]);
-      c.d(c.L.D + 4 * J + r) = double(inv[r]);
+      for (int s = 0; s <= r; ++s) c.template x<RC>(tJJ + 4 * r + s) = a[r][s];
+      c.template x<RC>(c.L.D + 4 * J + r) = inv[r];
     }
     for (int I = J + 1; I < nT; ++I) {
       const int tIJ = M + tile(I, J);
       RC b[4][4];
 #pragma unroll
-      for (int e = 0; e < 16; ++e) b[e >> 2][e & 3] = RC(c.d(tIJ + e));
+      for (int e = 0; e < 16; ++e) b[e >> 2][e & 3] = (c.template x<RC>(tIJ + e));
       for (int K = 0; K < J; ++K) {
         const int tIK = M + tile(I, K), tJK = M + tile(J, K);
         RC x[4][4], y[4][4];
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
-          x[e >> 2][e & 3] = RC(c.d(tIK + e));
-          y[e >> 2][e & 3] = RC(c.d(tJK + e));
+          x[e >> 2][e & 3] = (c.template x<RC>(tIK + e));
+          y[e >> 2][e & 3] = (c.template x<RC>(tJK + e));
         }
 #pragma unroll
         for (int r = 0; r < 4; ++r)
@@ -275,67 +289,76 @@ __device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& c, Col<double>
           b[r][s] = x * inv[s];
         }
 #pragma unroll
-      for (int e = 0; e < 16; ++e) c.d(tIJ + e) = double(b[e >> 2][e & 3]);
+      for (int e = 0; e < 16; ++e) c.template x<RC>(tIJ + e) = b[e >> 2][e & 3];
     }
   }
+  lane_solve<R, RC>(c);
+  for (int i = 0; i < nv; ++i) {
+    const double x = double(c.template x<RC>(c.L.rhs + i));
+    qdd[i] = x;
+    if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
+  }
+  return st;
+}
+
+// The two triangular solves with the factor left in M / D by
+// lane_cholesky_solve, in place on the (padded) rhs vector.
+template <typename R, typename RC>
+__device__ __noinline__ void lane_solve(const LaneCtx<R>& c) {
+  const int nT = (c.nv + 3) >> 2;
+  const int M = c.L.M;
   // forward substitution L y = rhs
   for (int I = 0; I < nT; ++I) {
     RC y[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) y[r] = RC(c.d(c.L.rhs + 4 * I + r));
+    for (int r = 0; r < 4; ++r) y[r] = (c.template x<RC>(c.L.rhs + 4 * I + r));
     for (int K = 0; K < I; ++K) {
       const int tIK = M + tile(I, K);
       RC z[4];
 #pragma unroll
-      for (int m = 0; m < 4; ++m) z[m] = RC(c.d(c.L.rhs + 4 * K + m));
+      for (int m = 0; m < 4; ++m) z[m] = (c.template x<RC>(c.L.rhs + 4 * K + m));
 #pragma unroll
       for (int r = 0; r < 4; ++r)
-        y[r] -= (RC(c.d(tIK + 4 * r)) * z[0] + RC(c.d(tIK + 4 * r + 1)) * z[1]) +
-                (RC(c.d(tIK + 4 * r + 2)) * z[2] + RC(c.d(tIK + 4 * r + 3)) * z[3]);
+        y[r] -= ((c.template x<RC>(tIK + 4 * r)) * z[0] + (c.template x<RC>(tIK + 4 * r + 1)) * z[1]) +
+                ((c.template x<RC>(tIK + 4 * r + 2)) * z[2] + (c.template x<RC>(tIK + 4 * r + 3)) * z[3]);
     }
     const int tII = M + tile(I, I);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       RC x = y[r];
 #pragma unroll
-      for (int m = 0; m < r; ++m) x -= RC(c.d(tII + 4 * r + m)) * y[m];
-      y[r] = x * RC(c.d(c.L.D + 4 * I + r));
+      for (int m = 0; m < r; ++m) x -= (c.template x<RC>(tII + 4 * r + m)) * y[m];
+      y[r] = x * (c.template x<RC>(c.L.D + 4 * I + r));
     }
 #pragma unroll
-    for (int r = 0; r < 4; ++r) c.d(c.L.rhs + 4 * I + r) = double(y[r]);
+    for (int r = 0; r < 4; ++r) c.template x<RC>(c.L.rhs + 4 * I + r) = y[r];
   }
   // back substitution Lᵀ x = y
   for (int I = nT - 1; I >= 0; --I) {
     RC x[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) x[r] = RC(c.d(c.L.rhs + 4 * I + r));
+    for (int r = 0; r < 4; ++r) x[r] = (c.template x<RC>(c.L.rhs + 4 * I + r));
     for (int K = I + 1; K < nT; ++K) {
       const int tKI = M + tile(K, I);
       RC z[4];
 #pragma unroll
-      for (int m = 0; m < 4; ++m) z[m] = RC(c.d(c.L.rhs + 4 * K + m));
+      for (int m = 0; m < 4; ++m) z[m] = (c.template x<RC>(c.L.rhs + 4 * K + m));
 #pragma unroll
       for (int r = 0; r < 4; ++r)
-        x[r] -= (RC(c.d(tKI + r)) * z[0] + RC(c.d(tKI + 4 + r)) * z[1]) +
-                (RC(c.d(tKI + 8 + r)) * z[2] + RC(c.d(tKI + 12 + r)) * z[3]);
+        x[r] -= ((c.template x<RC>(tKI + r)) * z[0] + (c.template x<RC>(tKI + 4 + r)) * z[1]) +
+                ((c.template x<RC>(tKI + 8 + r)) * z[2] + (c.template x<RC>(tKI + 12 + r)) * z[3]);
     }
     const int tII = M + tile(I, I);
 #pragma unroll
     for (int r = 3; r >= 0; --r) {
       RC v = x[r];
 #pragma unroll
-      for (int m = r + 1; m < 4; ++m) v -= RC(c.d(tII + 4 * m + r)) * x[m];
-      x[r] = v * RC(c.d(c.L.D + 4 * I + r));
+      for (int m = r + 1; m < 4; ++m) v -= (c.template x<RC>(tII + 4 * m + r)) * x[m];
+      x[r] = v * (c.template x<RC>(c.L.D + 4 * I + r));
     }
 #pragma unroll
-    for (int r = 0; r < 4; ++r) c.d(c.L.rhs + 4 * I + r) = double(x[r]);
+    for (int r = 0; r < 4; ++r) c.template x<RC>(c.L.rhs + 4 * I + r) = x[r];
   }
-  for (int i = 0; i < nv; ++i) {
-    const double x = c.d(c.L.rhs + i);
-    qdd[i] = x;
-    if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
-  }
-  return st;
 }
 
 // One dynamics evaluation (src/dynamics.rs:322-364): reads q, v, tau (double
@@ -396,10 +419,9 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
     if (type == 1 || type == 2) {  // revolute / prismatic
       V3<R> ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
       V3<R> aw = mul(Am, ax);  // world axis (R_b a = A a)
-      R qv = R(q[qo]);
       if (type == 1) {
         R s, co;
-        sincos_r<R>(qv, &s, &co);
+        sincos_q<R>(q[qo], &s, &co);
         if (fl & BF_AXIS_PRINCIPAL) {
           int ai = bf_axis_index(fl);
           R sg = (fl & BF_AXIS_NEG) ? -s : s;
@@ -427,7 +449,7 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
         S[0] = {aw, cross(pb, aw)};
       } else {
         Rb = Am;
-        pb = pb + aw * qv;
+        pb = pb + aw * R(q[qo]);
         S[0] = {{R(0), R(0), R(0)}, aw};
       }
       nvb = 1;
@@ -527,7 +549,7 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
     // from the previous evaluation: clear the tiled triangle first.
     const int nT = (nv + 3) >> 2;
     const int nm = (nT * (nT + 1) >> 1) * 16;
-    for (int e = 0; e < nm; ++e) c.d(c.L.M + e) = 0.0;
+    for (int e = 0; e < nm; ++e) c.template x<RC>(c.L.M + e) = RC(0);
   }
   SI<R> cI;
   SV<R> cF;
@@ -550,13 +572,14 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
         double ks = double(c.t(tb + TD_SPRING)), ls = double(c.t(tb + TD_SPRING + 1));
         rhs += -ks * (q[qo] - ls);
       }
-      c.d(c.L.rhs + vo + k) = rhs - double(sdot(Sk, f));
+      // right-hand side kept in the factorisation's precision
+      c.template x<RC>(c.L.rhs + vo + k) = RC(RC(rhs) - RC(sdot(Sk, f)));
       SV<R> Fk = imul(Ic, Sk);
       // row vo+k of H: F_kᵀ S_l for every column l of this joint and its ancestors
       const int row = vo + k;
       for (int l = 0; l <= k; ++l) {
         SV<R> Sl = l == k ? Sk : load_sv(c, c.L.S + 6 * (vo + l));
-        c.d(c.L.M + tix(row, vo + l)) = double(sdot2(Fk, Sl));
+        c.template x<RC>(c.L.M + tix(row,vo + l)) = RC(sdot2(Fk, Sl));
       }
       int a = parent;
       while (a != 0) {
@@ -565,7 +588,7 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
         int nva = ta == 3 ? 6 : (ta == 0 ? 0 : 1);
         for (int l = 0; l < nva; ++l) {
           SV<R> Sl = load_sv(c, c.L.S + 6 * (voa + l));
-          c.d(c.L.M + tix(row, voa + l)) = double(sdot2(Fk, Sl));
+          c.template x<RC>(c.L.M + tix(row,voa + l)) = RC(sdot2(Fk, Sl));
         }
         a = (wa >> 4) & 255;
       }
@@ -592,6 +615,52 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
   return lane_cholesky_solve<R, RC>(c, qdd);
 }
 
+#include "gpb_link.cuh"
+
+// MIXED_REFINED: the link-coordinate sweep in FP32 (bias forces, mass matrix,
+// Cholesky) gives x0; iterative refinement then solves H δ = τ − ID(q, q̇, x0)
+// with the FP32 factor, the residual coming from the same sweep in FP64 without
+// the mass matrix, and returns x0 + δ.  The error contracts from e0 ≈ cond·ε32
+// by a factor κ ≈ cond·ε32 per step (κ reaches 1e-2 on 48-body chains); a
+// second step runs only where the first correction exceeded 1e-4 of max(|q̈|, 1).
+// The O(n²)/O(n³) work (fill, factor, solves) stays on the FP32 pipe; the FP64
+// pipe does the O(n) residual.
+template <typename RC>
+__device__ __forceinline__ int refine(const LaneCtx<float>& c, const LaneCtx<double>& c2, Col<double> q,
+                                      Col<double> v, Col<double> tau, bool have_tau, Col<double> qdd,
+                                      Col<double> cf, bool want_cf) {
+  int st = 0;
+  for (int it = 0; it < 2; ++it) {
+    lane_link<double, RC, true>(c2, q, v, tau, have_tau, qdd, qdd, cf, want_cf && it == 0);
+    lane_solve<float, RC>(c);
+    double dmax = 0.0, xmax = 1.0;
+    for (int i = 0; i < c.nv; ++i) {
+      const double d = double(c.template x<RC>(c.L.rhs + i));
+      const double x = qdd[i] + d;
+      qdd[i] = x;
+      dmax = fmax(dmax, fabs(d));
+      xmax = fmax(xmax, fabs(x));
+      if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
+    }
+    if (st || !(dmax > 1e-4 * xmax)) break;
+  }
+  return st;
+}
+__device__ __noinline__ int lane_dynamics_refined(const LaneCtx<float>& c, const LaneCtx<double>& c2,
+                                                  Col<double> q, Col<double> v, Col<double> tau,
+                                                  bool have_tau, Col<double> qdd, Col<double> cf,
+                                                  bool want_cf) {
+  Col<double> none{nullptr};
+  int st = lane_link<float, float, false>(c, q, v, tau, have_tau, none, qdd, none, false);
+  if (st & 2) {  // FP32 factorisation broke down: factor the same matrix in FP64
+    st = lane_link<float, double, false>(c, q, v, tau, have_tau, none, qdd, none, false);
+    if (st) return st;
+    return refine<double>(c, c2, q, v, tau, have_tau, qdd, cf, want_cf);
+  }
+  if (st) return st;
+  return refine<float>(c, c2, q, v, tau, have_tau, qdd, cf, want_cf);
+}
+
 // quaternion_derivative (src/util.rs:83-102) and the pose update of
 // euler_step / compute_new_q (src/integrators.rs:247-258,303-313).
 __device__ __forceinline__ void pose_advance(Col<double> q, int qo, const double* vel, double dt,
@@ -607,7 +676,7 @@ __device__ __forceinline__ void pose_advance(Col<double> q, int qo, const double
   V3<double> td = mul(Rq, V3<double>{vel[3], vel[4], vel[5]});
   double tx = q[qo + 4] + td.x * dt, ty = q[qo + 5] + td.y * dt, tz = q[qo + 6] + td.z * dt;
   double nx = x + dx * dt, ny = y + dy * dt, nz = z + dz * dt, nw = w + dw * dt;
-  double inv = 1.0 / sqrt(nx * nx + ny * ny + nz * nz + nw * nw);
+  double inv = 1.0 / ::sqrt(nx * nx + ny * ny + nz * nz + nw * nw);
   qn[qo] = nx * inv;
   qn[qo + 1] = ny * inv;
   qn[qo + 2] = nz * inv;
@@ -635,17 +704,42 @@ __device__ __forceinline__ void advance_q(const LaneCtx<R>& c, Col<double> q, Co
   }
 }
 
-template <typename R, typename RC>
-__device__ int lane_step(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<double> tau,
+// Dynamics evaluators of the three precision modes (q, v, τ → q̈).
+struct EvalFP64 {
+  LaneCtx<double> c;
+  __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
+                            Col<double> cf = Col<double>{nullptr}, bool want_cf = false) const {
+    return lane_dynamics<double, double>(c, q, v, t, ht, x, cf, want_cf);
+  }
+};
+struct EvalMixed {  // FP32 sweeps and fill; FP64 Cholesky when n > 12
+  LaneCtx<float> c;
+  __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
+                            Col<double> cf = Col<double>{nullptr}, bool want_cf = false) const {
+    if (c.nv <= 12) return lane_dynamics<float, float>(c, q, v, t, ht, x, cf, want_cf);
+    return lane_dynamics<float, double>(c, q, v, t, ht, x, cf, want_cf);
+  }
+};
+struct EvalRefined {  // FP32 solve + FP64 residual refinement
+  LaneCtx<float> c;
+  LaneCtx<double> cd;
+  __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
+                            Col<double> cf = Col<double>{nullptr}, bool want_cf = false) const {
+    return lane_dynamics_refined(c, cd, q, v, t, ht, x, cf, want_cf);
+  }
+};
+
+template <typename E>
+__device__ int lane_step(const E& ev, Col<double> q, Col<double> v, Col<double> tau,
                          bool have_tau, double dt, int integrator) {
+  const auto& c = ev.c;
   const int nv = c.nv;
   Col<double> f{&c.d(c.L.facc)};
   Col<double> qs{&c.d(c.L.qs)}, vs{&c.d(c.L.vs)};
   Col<double> tmp{&c.d(c.L.v0)};
-  Col<double> none{nullptr};
   int st = 0;
   if (integrator == 0) {  // semi-implicit Euler (src/integrators.rs:25-39,276-319)
-    st |= lane_dynamics<R, RC>(c, q, v, tau, have_tau, tmp, none, false);
+    st |= ev(q, v, tau, have_tau, tmp);
     if (st) return st;
     for (int i = 0; i < nv; ++i) v[i] = v[i] + tmp[i] * dt;
     advance_q(c, q, v, dt, q);
@@ -656,12 +750,12 @@ __device__ int lane_step(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<
   // q is not written before the last stage, so it serves as q0.
   Col<double> q0 = q;
   Col<double> k1{&c.d(c.L.v0)};
-  st |= lane_dynamics<R, RC>(c, q, v, tau, have_tau, k1, none, false);
+  st |= ev(q, v, tau, have_tau, k1);
   if (st) return st;
   if (integrator == 1) {  // RK2
     for (int i = 0; i < nv; ++i) vs[i] = v[i] + k1[i] * (dt / 2.0);
     advance_q(c, q0, v, dt / 2.0, qs);
-    st |= lane_dynamics<R, RC>(c, qs, vs, tau, have_tau, k1, none, false);
+    st |= ev(qs, vs, tau, have_tau, k1);
     if (st) return st;
     advance_q(c, q0, v, dt, q);
     for (int i = 0; i < nv; ++i) v[i] = v[i] + k1[i] * dt;
@@ -673,21 +767,21 @@ __device__ int lane_step(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<
     vs[i] = v[i] + k1[i] * (dt / 2.0);
   }
   advance_q(c, q0, v, dt / 2.0, qs);
-  st |= lane_dynamics<R, RC>(c, qs, vs, tau, have_tau, k1, none, false);
+  st |= ev(qs, vs, tau, have_tau, k1);
   if (st) return st;
   for (int i = 0; i < nv; ++i) {
     f[i] = f[i] + k1[i] * 2.0;
     vs[i] = v[i] + k1[i] * (dt / 2.0);
   }
   // qs already equals q0 + dt/2 · v0
-  st |= lane_dynamics<R, RC>(c, qs, vs, tau, have_tau, k1, none, false);
+  st |= ev(qs, vs, tau, have_tau, k1);
   if (st) return st;
   for (int i = 0; i < nv; ++i) {
     f[i] = f[i] + k1[i] * 2.0;
     vs[i] = v[i] + k1[i] * dt;
   }
   advance_q(c, q0, v, dt, qs);
-  st |= lane_dynamics<R, RC>(c, qs, vs, tau, have_tau, k1, none, false);
+  st |= ev(qs, vs, tau, have_tau, k1);
   if (st) return st;
   for (int i = 0; i < nv; ++i) f[i] = (f[i] + k1[i]) / 6.0;
   advance_q(c, q0, v, dt, q);
@@ -715,6 +809,7 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   c.L = scratch_layout(pd.nb, pd.nq, pd.nv, pd.nc);
   c.sD = b.scratch + pd.scr * LANES + lane;
   c.sR = reinterpret_cast<R*>(b.scratch + pd.scr * LANES) + lane;
+  c.s0 = reinterpret_cast<char*>(b.scratch + pd.scr * LANES);
   return c;
 }
 
@@ -744,10 +839,30 @@ __device__ __forceinline__ bool control(const LaneCtx<R>& c, const DeviceBatch& 
   return p.tau_mode != 0;  // host torques live in tin
 }
 
-template <typename R, typename RCsmall>
+template <int PREC>
+struct EvalOf;
+template <>
+struct EvalOf<0> {
+  __device__ static EvalFP64 make(const DeviceBatch& b, const PackDesc& pd, int lane) {
+    return EvalFP64{make_ctx<double>(b, pd, lane)};
+  }
+};
+template <>
+struct EvalOf<1> {
+  __device__ static EvalMixed make(const DeviceBatch& b, const PackDesc& pd, int lane) {
+    return EvalMixed{make_ctx<float>(b, pd, lane)};
+  }
+};
+template <>
+struct EvalOf<2> {
+  __device__ static EvalRefined make(const DeviceBatch& b, const PackDesc& pd, int lane) {
+    return EvalRefined{make_ctx<float>(b, pd, lane), make_ctx<double>(b, pd, lane)};
+  }
+};
+
+template <int PREC>
 __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams p) {
   const int lane = threadIdx.x & 31;
-  const int warps_per_block = blockDim.x >> 5;
   while (true) {
     int pk = 0;
     if (lane == 0) pk = atomicAdd(b.queue, 1);
@@ -755,24 +870,20 @@ __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams
     if (pk >= b.npacks) break;
     const PackDesc pd = b.packs[pk];
     if (lane >= pd.count) continue;
-    LaneCtx<R> c = make_ctx<R>(b, pd, lane);
+    const auto ev = EvalOf<PREC>::make(b, pd, lane);
+    const auto& c = ev.c;
     int32_t* status = b.status + (int64_t)pk * LANES + lane;
     const int64_t inst = b.laneI[pd.lane * LANES + lane];
     Col<double> q = col_at(b.q, pd.q, lane), v = col_at(b.v, pd.v, lane);
     Col<double> tin = col_at(b.tau_in, pd.v, lane);
     Col<double> tau{&c.d(c.L.tau)};
-    const bool small = c.nv <= 12;
     int64_t done = 0;  // steps this instance completed in this launch
     for (int64_t s = 0; s < p.K; ++s) {
       if (*status) break;
       const int64_t sidx = p.step0 + s;
       bool ht = control(c, b, p, inst, sidx, s == 0, q, v, tin, tau);
       Col<double> tsrc = p.control == 0 ? tin : tau;
-      int st;
-      if (p.precision == 1 && small)
-        st = lane_step<R, RCsmall>(c, q, v, tsrc, ht, p.dt, p.integrator);
-      else
-        st = lane_step<R, double>(c, q, v, tsrc, ht, p.dt, p.integrator);
+      const int st = lane_step(ev, q, v, tsrc, ht, p.dt, p.integrator);
       if (st) {
         *status = st;
         break;
@@ -790,27 +901,23 @@ __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams
     }
     b.done[(int64_t)pk * LANES + lane] = done;
   }
-  (void)warps_per_block;
 }
 
-template <typename R>
+template <int PREC>
 __global__ void __launch_bounds__(128) dynamics_kernel(DeviceBatch b, StepParams p) {
   const int lane = threadIdx.x & 31;
   const int pk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (pk >= b.npacks) return;
   const PackDesc pd = b.packs[pk];
   if (lane >= pd.count) return;
-  LaneCtx<R> c = make_ctx<R>(b, pd, lane);
+  const auto ev = EvalOf<PREC>::make(b, pd, lane);
+  const auto& c = ev.c;
   Col<double> q = col_at(b.q, pd.q, lane), v = col_at(b.v, pd.v, lane);
   Col<double> tin = col_at(b.tau_in, pd.v, lane);
   Col<double> qdd{&c.d(c.L.facc)};
   Col<double> cf{&c.d(c.L.cf)};
   for (int k = 0; k < 3 * c.nc; ++k) cf[k] = 0.0;
-  int st;
-  if (p.precision == 1 && c.nv <= 12)
-    st = lane_dynamics<R, float>(c, q, v, tin, p.tau_mode != 0, qdd, cf, true);
-  else
-    st = lane_dynamics<R, double>(c, q, v, tin, p.tau_mode != 0, qdd, cf, true);
+  const int st = ev(q, v, tin, p.tau_mode != 0, qdd, cf, true);
   b.status[(int64_t)pk * LANES + lane] |= st;
   const int64_t* vm = b.vmap + pd.v * LANES + lane;
   for (int i = 0; i < c.nv; ++i) p.qdd_out[vm[(size_t)i * LANES]] = qdd[i];
@@ -842,20 +949,16 @@ cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes
   if (e != cudaSuccess) return e;
   const int threads = 128;
   int per_sm = 0;
-  if (p.precision == 1)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, simulate_kernel<float, float>, threads, 0);
-  else
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, simulate_kernel<double, double>, threads, 0);
+  auto kern = p.precision == 2 ? simulate_kernel<2>
+                               : (p.precision == 1 ? simulate_kernel<1> : simulate_kernel<0>);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   int64_t want = (b.npacks + (threads / 32) - 1) / (threads / 32);
   int64_t grid = (int64_t)num_sms * per_sm;
   if (grid > want) grid = want;
   if (grid < 1) grid = 1;
-  if (p.precision == 1)
-    simulate_kernel<float, float><<<(unsigned)grid, threads, 0, s>>>(b, p);
-  else
-    simulate_kernel<double, double><<<(unsigned)grid, threads, 0, s>>>(b, p);
+  kern<<<(unsigned)grid, threads, 0, s>>>(b, p);
   return cudaGetLastError();
 }
 
@@ -863,10 +966,9 @@ cudaError_t launch_dynamics(const DeviceBatch& b, const StepParams& p, cudaStrea
   const int threads = 128;
   unsigned grid = (unsigned)((b.npacks + 3) / 4);
   if (grid == 0) return cudaSuccess;
-  if (p.precision == 1)
-    dynamics_kernel<float><<<grid, threads, 0, s>>>(b, p);
-  else
-    dynamics_kernel<double><<<grid, threads, 0, s>>>(b, p);
+  auto kern = p.precision == 2 ? dynamics_kernel<2>
+                               : (p.precision == 1 ? dynamics_kernel<1> : dynamics_kernel<0>);
+  kern<<<grid, threads, 0, s>>>(b, p);
   return cudaGetLastError();
 }
 
@@ -930,14 +1032,15 @@ static cudaError_t static_scratch_address(int device, double** out) {
 // static scratch (the q / v / τ slots of each instance's scratch layout).
 template <typename R>
 __global__ void __launch_bounds__(128)
-    dynamics_static_kernel(DeviceBatch b, int precision, const double* qu, const double* vu,
+    dynamics_static_kernel(DeviceBatch b, const double* qu, const double* vu,
                            const double* tu, double* qddu) {
   const int lane = threadIdx.x & 31;
   const int pk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (pk >= b.npacks) return;
   const PackDesc pd = b.packs[pk];
   if (lane >= pd.count) return;
-  LaneCtx<R> c = make_ctx<R>(b, pd, lane);
+  const auto ev = EvalOf<R::value>::make(b, pd, lane);
+  const auto& c = ev.c;
   Col<double> q{&c.d(c.L.qs)}, v{&c.d(c.L.vs)}, tau{&c.d(c.L.tau)}, qdd{&c.d(c.L.facc)};
   const int64_t* qm = b.qmap + pd.q * LANES + lane;
   const int64_t* vm = b.vmap + pd.v * LANES + lane;
@@ -946,12 +1049,7 @@ __global__ void __launch_bounds__(128)
     v[i] = vu[vm[(size_t)i * LANES]];
     tau[i] = tu ? tu[vm[(size_t)i * LANES]] : 0.0;
   }
-  Col<double> none{nullptr};
-  int st;
-  if (precision == 1 && c.nv <= 12)
-    st = lane_dynamics<R, float>(c, q, v, tau, true, qdd, none, false);
-  else
-    st = lane_dynamics<R, double>(c, q, v, tau, true, qdd, none, false);
+  const int st = ev(q, v, tau, true, qdd);
   b.status[(int64_t)pk * LANES + lane] |= st;
   for (int i = 0; i < c.nv; ++i) qddu[vm[(size_t)i * LANES]] = qdd[i];
 }
@@ -969,9 +1067,11 @@ cudaError_t launch_dynamics_static(const DeviceBatch& batch, int device, int64_t
   unsigned grid = (unsigned)((b.npacks + 3) / 4);
   if (grid == 0) return cudaSuccess;
   if (precision == 1)
-    dynamics_static_kernel<float><<<grid, threads, 0, s>>>(b, precision, q, v, tau, qdd);
+    dynamics_static_kernel<std::integral_constant<int, 1>><<<grid, threads, 0, s>>>(b, q, v, tau, qdd);
+  else if (precision == 2)
+    dynamics_static_kernel<std::integral_constant<int, 2>><<<grid, threads, 0, s>>>(b, q, v, tau, qdd);
   else
-    dynamics_static_kernel<double><<<grid, threads, 0, s>>>(b, precision, q, v, tau, qdd);
+    dynamics_static_kernel<std::integral_constant<int, 0>><<<grid, threads, 0, s>>>(b, q, v, tau, qdd);
   return cudaGetLastError();
 }
 

@@ -72,7 +72,7 @@ __host__ __device__ inline double polar_normal(uint32_t key0, uint32_t key1, uin
     double u2 = fma(b, scale, -1.0);
     double s = fma(u1, u1, u2 * u2);
     if (s >= 1.0 || s == 0.0) continue;
-    return u1 * sqrt((-2.0 * det_log(s)) / s);
+    return u1 * ::sqrt((-2.0 * det_log(s)) / s);
   }
   return 0.0;
 }

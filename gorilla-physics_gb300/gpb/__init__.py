@@ -5,7 +5,7 @@ All arithmetic runs in the CUDA kernels of libgpb.so (sm_103a); this package
 only describes mechanisms and calls the C ABI of include/gpb.h.
 """
 
-from ._abi import (FIXED, FLOATING, FP64, HUNT_CROSSLEY, LINEAR_SPRING_DAMPER, MIXED, PRISMATIC,
+from ._abi import (FIXED, FLOATING, FP64, HUNT_CROSSLEY, LINEAR_SPRING_DAMPER, MIXED, MIXED_REFINED, PRISMATIC,
                    REVOLUTE, RUNGE_KUTTA_2, RUNGE_KUTTA_4, SEMI_IMPLICIT_EULER, GpbError, lib)
 from .batch import Batch, Context, Integrator, Precision, simulate, simulate_steps
 from .model import (WORLD_FRAME, ContactPoint, FixedJoint, FloatingJoint, HalfSpace,

@@ -17,7 +17,7 @@ GPB_E_INVAL, GPB_E_NOMEM, GPB_E_CUDA, GPB_E_TIMEOUT, GPB_E_RANGE, GPB_E_STATE = 
 GPB_ST_NONFINITE, GPB_ST_CHOL_FAIL = 1, 2
 FIXED, REVOLUTE, PRISMATIC, FLOATING = 0, 1, 2, 3
 SEMI_IMPLICIT_EULER, RUNGE_KUTTA_2, RUNGE_KUTTA_4 = 0, 1, 2
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_REFINED = 0, 1, 2
 HUNT_CROSSLEY, LINEAR_SPRING_DAMPER = 0, 1
 CONTROL_HOST_TAU, CONTROL_OPEN_LOOP, CONTROL_PD = 0, 1, 2
 MAX_BODIES = MAX_DOF = MAX_CONTACTS = 64

@@ -76,8 +76,12 @@ enum gpb_integrator {
 
 /* GPB_FP64: every quantity in FP64 (the drop-in).  GPB_MIXED: sweeps, contact
  * and mass-matrix build in FP32; FP64 position/quaternion accumulator; FP64
- * Cholesky when n > 12. */
-enum gpb_precision { GPB_FP64 = 0, GPB_MIXED = 1 };
+ * Cholesky when n > 12.  GPB_MIXED_REFINED: bias forces, mass matrix and
+ * Cholesky of one evaluation in FP32 (link coordinates), then iterative
+ * refinement whose residual τ − ID(q, q̇, q̈₀) is a link-coordinate
+ * Newton–Euler pass in FP64 (a second step only where the first correction
+ * exceeds 1e-4 of max(|q̈|, 1)); FP64 position/quaternion accumulator. */
+enum gpb_precision { GPB_FP64 = 0, GPB_MIXED = 1, GPB_MIXED_REFINED = 2 };
 
 /* GPB_HUNT_CROSSLEY: src/contact.rs:260-338 (k = k_p k_h/(k_p+k_h), k_h = 50e3,
  * π = max(λ z^1.5 ż + k z^1.5, 0), λ = 1.5 α k).
