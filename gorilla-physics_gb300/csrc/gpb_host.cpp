@@ -79,6 +79,7 @@ struct gpb_batch {
   int64_t n = 0;
   int32_t npacks = 0;
   int mapping = 0;
+  int warps_per_sm = 0;  // resident warps per SM of the step kernel (0 = occupancy limit)
   std::vector<int64_t> q_off, v_off, c_off;  // user layout, [n+1]
   int64_t nq_total = 0, nv_total = 0, nc_total = 0;
   std::vector<PackDesc> packs_h;
@@ -533,6 +534,14 @@ extern "C" int gpb_batch_set_mapping(gpb_batch* b, int lanes) {
   return GPB_OK;
 }
 
+extern "C" int gpb_batch_set_launch(gpb_batch* b, int warps_per_sm) {
+  if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_launch: batch is NULL");
+  if (warps_per_sm < 0 || warps_per_sm > 64 || warps_per_sm % 4 != 0)
+    return fail(GPB_E_INVAL, "gpb_batch_set_launch: warps_per_sm must be 0 or a multiple of 4 up to 64");
+  b->warps_per_sm = warps_per_sm;
+  return GPB_OK;
+}
+
 static int upload_user(gpb_batch* b, const double* src, int64_t count, DBuf<double>& stage,
                        const DBuf<int64_t>& map, int64_t slots, DBuf<double>& dst) {
   cudaStream_t s = b->ctx->stream;
@@ -653,7 +662,7 @@ static int run_simulate(gpb_batch* b, double dt, int64_t K, int64_t step0, int i
   }
   if (b->npacks > 0 && K > 0) {
     CUDA_TRY(cudaEventRecord(b->ctx->ev0, s));
-    CUDA_TRY(launch_simulate(b->dev(), p, b->mapping, b->ctx->num_sms, s));
+    CUDA_TRY(launch_simulate(b->dev(), p, b->mapping, b->ctx->num_sms, b->warps_per_sm, s));
     CUDA_TRY(cudaEventRecord(b->ctx->ev1, s));
     b->ctx->timed = true;
     b->ctx->launches++;

@@ -206,7 +206,8 @@ __device__ __noinline__ void lane_solve(const LaneCtx<R>& c);
 // the solves L y = rhs, Lᵀ x = y.  n is padded to a multiple of 4 with identity
 // rows.  Writes q̈ into `qdd`; returns GPB status bits.
 template <typename R, typename RC>
-__device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& c, Col<double> qdd) {
+__device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& cin, Col<double> qdd) {
+  const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
   const int nv = c.nv, nT = (nv + 3) >> 2, np = nT << 2;
   const int M = c.L.M;
   for (int i = nv; i < np; ++i) {
@@ -292,7 +293,7 @@ __device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& c, Col<double>
       for (int e = 0; e < 16; ++e) c.template x<RC>(tIJ + e) = b[e >> 2][e & 3];
     }
   }
-  lane_solve<R, RC>(c);
+  lane_solve<R, RC>(cin);
   for (int i = 0; i < nv; ++i) {
     const double x = double(c.template x<RC>(c.L.rhs + i));
     qdd[i] = x;
@@ -304,7 +305,8 @@ __device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& c, Col<double>
 // The two triangular solves with the factor left in M / D by
 // lane_cholesky_solve, in place on the (padded) rhs vector.
 template <typename R, typename RC>
-__device__ __noinline__ void lane_solve(const LaneCtx<R>& c) {
+__device__ __noinline__ void lane_solve(const LaneCtx<R>& cin) {
+  const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
   const int nT = (c.nv + 3) >> 2;
   const int M = c.L.M;
   // forward substitution L y = rhs
@@ -364,8 +366,9 @@ __device__ __noinline__ void lane_solve(const LaneCtx<R>& c) {
 // One dynamics evaluation (src/dynamics.rs:322-364): reads q, v, tau (double
 // columns), writes q̈ into `qdd`.  Returns GPB status bits.
 template <typename R, typename RC>
-__device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<double> tau,
+__device__ __noinline__ int lane_dynamics(const LaneCtx<R>& cin, Col<double> q, Col<double> v, Col<double> tau,
                              bool have_tau, Col<double> qdd, Col<double> cforce, bool want_cf) {
+  const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
   const R g = R(GRAVITY);
   // ---- outward sweep --------------------------------------------------
   M3<R> Rp;
@@ -612,7 +615,7 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
     }
   }
 
-  return lane_cholesky_solve<R, RC>(c, qdd);
+  return lane_cholesky_solve<R, RC>(cin, qdd);
 }
 
 #include "gpb_link.cuh"
@@ -943,7 +946,7 @@ __global__ void gather_kernel(const int64_t* map, int64_t slots, const double* s
 }
 
 cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes_per_instance,
-                            int num_sms, cudaStream_t s) {
+                            int num_sms, int warps_per_sm, cudaStream_t s) {
   (void)lanes_per_instance;
   cudaError_t e = cudaMemsetAsync(b.queue, 0, sizeof(int32_t), s);
   if (e != cudaSuccess) return e;
@@ -953,6 +956,7 @@ cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes
                                : (p.precision == 1 ? simulate_kernel<1> : simulate_kernel<0>);
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
   if (e != cudaSuccess) return e;
+  if (warps_per_sm > 0 && warps_per_sm / (threads / 32) < per_sm) per_sm = warps_per_sm / (threads / 32);
   if (per_sm < 1) per_sm = 1;
   int64_t want = (b.npacks + (threads / 32) - 1) / (threads / 32);
   int64_t grid = (int64_t)num_sms * per_sm;

@@ -56,9 +56,10 @@ __device__ __forceinline__ void load_rel(const LaneCtx<R>& c, int b, M3<R>& Rr, 
 // RESIDUAL = false: q̈ into qdd (returns status bits).  RESIDUAL = true: the
 // residual at ẍ = xacc into the scratch rhs vector (in RC), returns 0.
 template <typename R, typename RC, bool RESIDUAL>
-__device__ __noinline__ int lane_link(const LaneCtx<R>& c, Col<double> q, Col<double> v,
+__device__ __noinline__ int lane_link(const LaneCtx<R>& cin, Col<double> q, Col<double> v,
                                       Col<double> tau, bool have_tau, Col<double> xacc,
                                       Col<double> qdd, Col<double> cf, bool want_cf) {
+  const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
   using V = V3<R>;
   const bool contacts = c.nc > 0;
   const V zero{R(0), R(0), R(0)};
@@ -336,5 +337,5 @@ __device__ __noinline__ int lane_link(const LaneCtx<R>& c, Col<double> q, Col<do
     }
   }
   if (RESIDUAL) return 0;
-  return lane_cholesky_solve<R, RC>(c, qdd);
+  return lane_cholesky_solve<R, RC>(cin, qdd);
 }

@@ -155,6 +155,10 @@ class Batch:
         _abi.check(_abi.lib().gpb_batch_set_mapping(self.h, lanes_per_instance),
                    "gpb_batch_set_mapping")
 
+    def set_launch(self, warps_per_sm: int) -> None:
+        """Resident warps per SM of the step kernel (0 = occupancy limit)."""
+        _abi.check(_abi.lib().gpb_batch_set_launch(self.h, warps_per_sm), "gpb_batch_set_launch")
+
     # -- the hot path -----------------------------------------------------------
     def dynamics_continuous(self, tau=None, precision: int = _abi.FP64,
                             contact_forces: bool = False):

@@ -264,6 +264,12 @@ int gpb_synchronize(gpb_ctx* ctx);
  */
 int gpb_batch_set_mapping(gpb_batch* batch, int lanes_per_instance);
 
+/* Resident warps per SM of the persistent step kernel (one warp per pack of
+ * 32 instances): 0 = as many as the kernel's registers allow (the default),
+ * else a multiple of 4 up to 64, capped by that limit.  With 4, each of the
+ * SM's four schedulers (each with its own FP64 unit) runs one pack at a time. */
+int gpb_batch_set_launch(gpb_batch* batch, int warps_per_sm);
+
 /* Number of this library's kernel launches issued by the context so far. */
 int64_t gpb_launch_count(const gpb_ctx* ctx);
 
