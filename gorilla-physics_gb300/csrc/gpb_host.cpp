@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "gpb.h"
+#include "gpb_host_impl.h"
 #include "gpb_internal.h"
 
 using namespace gpb;
@@ -27,126 +28,13 @@ using namespace gpb;
 
 static thread_local std::string g_last_error;
 
-static int fail(int code, const std::string& msg) {
+int gpb::fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;
 }
-#define CUDA_TRY(expr)                                                                    \
-  do {                                                                                    \
-    cudaError_t _e = (expr);                                                              \
-    if (_e != cudaSuccess)                                                                \
-      return fail(GPB_E_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));        \
-  } while (0)
 
 extern "C" int gpb_abi_version(void) { return GPB_ABI_VERSION; }
 extern "C" const char* gpb_last_error(void) { return g_last_error.c_str(); }
-
-// ---------------------------------------------------------------------------
-// device buffers
-
-template <typename T>
-struct DBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  cudaError_t alloc(size_t count) {
-    free();
-    n = count;
-    if (count == 0) return cudaSuccess;
-    return cudaMalloc(&p, count * sizeof(T));
-  }
-  void free() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  cudaError_t upload(const std::vector<T>& h, cudaStream_t s) {
-    if (h.empty()) return cudaSuccess;
-    return cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s);
-  }
-};
-
-struct gpb_ctx {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  int64_t launches = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the last simulate kernel
-  bool timed = false;
-};
-
-struct gpb_batch {
-  gpb_ctx* ctx = nullptr;
-  int64_t n = 0;
-  int32_t npacks = 0;
-  int mapping = 0;
-  int warps_per_sm = 0;  // resident warps per SM of the step kernel (0 = occupancy limit)
-  std::vector<int64_t> q_off, v_off, c_off;  // user layout, [n+1]
-  int64_t nq_total = 0, nv_total = 0, nc_total = 0;
-  std::vector<PackDesc> packs_h;
-  int64_t q_slots = 0, v_slots = 0, c_slots = 0;
-  int64_t scratch_words = 0;  // 8-byte words of per-instance scratch, all packs
-  std::vector<int32_t> status_slot;  // user instance -> status slot (pack*32+lane)
-  DBuf<PackDesc> packs;
-  DBuf<uint32_t> topoW;
-  DBuf<double> topoD, ctcD, hsD, q, v, tau_in, scratch, stage_q, stage_v, stage_c, hist;
-  DBuf<float> topoF, ctcF, hsF;
-  DBuf<int32_t> ctcI, laneI, status, queue;
-  DBuf<int64_t> qmap, vmap, cmap, done;
-  DeviceBatch dev() const {
-    DeviceBatch b;
-    b.npacks = npacks;
-    b.packs = packs.p;
-    b.topoW = topoW.p;
-    b.topoD = topoD.p;
-    b.topoF = topoF.p;
-    b.ctcI = ctcI.p;
-    b.ctcD = ctcD.p;
-    b.ctcF = ctcF.p;
-    b.hsD = hsD.p;
-    b.hsF = hsF.p;
-    b.laneI = laneI.p;
-    b.status = status.p;
-    b.done = done.p;
-    b.q = q.p;
-    b.v = v.p;
-    b.tau_in = tau_in.p;
-    b.scratch = scratch.p;
-    b.qmap = qmap.p;
-    b.vmap = vmap.p;
-    b.cmap = cmap.p;
-    b.nq_total = nq_total;
-    b.nv_total = nv_total;
-    b.nc_total = nc_total;
-    b.queue = queue.p;
-    return b;
-  }
-  void release() {
-    packs.free();
-    topoW.free();
-    topoD.free();
-    ctcD.free();
-    hsD.free();
-    q.free();
-    v.free();
-    tau_in.free();
-    scratch.free();
-    stage_q.free();
-    stage_v.free();
-    stage_c.free();
-    hist.free();
-    topoF.free();
-    ctcF.free();
-    hsF.free();
-    ctcI.free();
-    laneI.free();
-    status.free();
-    queue.free();
-    qmap.free();
-    vmap.free();
-    cmap.free();
-    done.free();
-  }
-};
 
 extern "C" int gpb_create(int device, gpb_ctx** out) {
   if (!out) return fail(GPB_E_INVAL, "gpb_create: out is NULL");
@@ -200,36 +88,47 @@ extern "C" int64_t gpb_launch_count(const gpb_ctx* ctx) { return ctx ? ctx->laun
 // ---------------------------------------------------------------------------
 // model validation and packing
 
-namespace {
 
-struct InstInfo {
-  int32_t j0, nb, nq, nv, c0, nc, h0, nh, model;
-  bool chain;
-  uint64_t sig;  // topology class
-};
-
-static int joint_nq(int t) { return t == GPB_JOINT_FLOATING ? 7 : (t == GPB_JOINT_FIXED ? 0 : 1); }
-static int joint_nv(int t) { return t == GPB_JOINT_FLOATING ? 6 : (t == GPB_JOINT_FIXED ? 0 : 1); }
-
-// Quaternion (x,y,z,w) → row-major rotation matrix (same formula as
-// UnitQuaternion::to_rotation_matrix).
-static void quat_to_rot(const double* q, double* m) {
-  double x = q[0], y = q[1], z = q[2], w = q[3];
-  double xx = x * x, yy = y * y, zz = z * z, ww = w * w;
-  double xy = x * y * 2, xz = x * z * 2, yz = y * z * 2, wx = w * x * 2, wy = w * y * 2,
-         wz = w * z * 2;
-  m[0] = ww + xx - yy - zz;
-  m[1] = xy - wz;
-  m[2] = xz + wy;
-  m[3] = xy + wz;
-  m[4] = ww - xx + yy - zz;
-  m[5] = yz - wx;
-  m[6] = xz - wy;
-  m[7] = yz + wx;
-  m[8] = ww - xx - yy + zz;
+int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
+  InstInfo& I = *out;
+  I.j0 = m->joint_offset[i];
+  I.nb = m->joint_offset[i + 1] - I.j0;
+  if (I.nb < 0 || I.nb > GPB_MAX_BODIES)
+    return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": body count outside [0, 64]");
+  I.nq = I.nv = 0;
+  I.chain = true;
+  uint64_t sig = 1469598103934665603ull;
+  for (int b = 0; b < I.nb; ++b) {
+    int t = m->joint_type[I.j0 + b], p = m->joint_parent[I.j0 + b];
+    if (t < 0 || t > 3) return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": bad joint type");
+    if (p < 0 || p > b)
+      return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": joint " + std::to_string(b + 1) +
+                                   " has parent " + std::to_string(p) + " (must be < its own number)");
+    if (p != b) I.chain = false;
+    I.nq += joint_nq(t);
+    I.nv += joint_nv(t);
+    sig = (sig ^ (uint64_t)(t * 131 + p)) * 1099511628211ull;
+  }
+  if (I.nv > GPB_MAX_DOF) return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": more than 64 DOF");
+  I.c0 = m->contact_offset ? m->contact_offset[i] : 0;
+  I.nc = m->contact_offset ? m->contact_offset[i + 1] - I.c0 : 0;
+  if (I.nc < 0 || I.nc > GPB_MAX_CONTACTS)
+    return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": contact count outside [0, 64]");
+  for (int k = 0; k < I.nc; ++k) {
+    int bb = m->contact_body[I.c0 + k];
+    if (bb < 1 || bb > I.nb) return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": contact on a missing body");
+  }
+  I.h0 = m->halfspace_offset ? m->halfspace_offset[i] : 0;
+  I.nh = m->halfspace_offset ? m->halfspace_offset[i + 1] - I.h0 : 0;
+  if (I.nh < 0 || I.nh > GPB_MAX_HALFSPACES)
+    return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": half-space count outside [0, 4]");
+  I.model = m->contact_model ? m->contact_model[i] : GPB_HUNT_CROSSLEY;
+  if (I.model != GPB_HUNT_CROSSLEY && I.model != GPB_LINEAR_SPRING_DAMPER)
+    return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": bad contact model");
+  sig = (sig ^ (uint64_t)(I.nc * 7 + I.nh)) * 1099511628211ull;
+  I.sig = sig;
+  return GPB_OK;
 }
-
-}  // namespace
 
 extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** out) {
   if (!ctx || !m || !out) return fail(GPB_E_INVAL, "gpb_batch_create: NULL argument");
@@ -239,45 +138,8 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
     return fail(GPB_E_INVAL, "gpb_batch_create: joint/body tables missing");
   const int64_t n = m->n_instances;
   std::vector<InstInfo> info(n);
-  for (int64_t i = 0; i < n; ++i) {
-    InstInfo& I = info[i];
-    I.j0 = m->joint_offset[i];
-    I.nb = m->joint_offset[i + 1] - I.j0;
-    if (I.nb < 0 || I.nb > GPB_MAX_BODIES)
-      return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": body count outside [0, 64]");
-    I.nq = I.nv = 0;
-    I.chain = true;
-    uint64_t sig = 1469598103934665603ull;
-    for (int b = 0; b < I.nb; ++b) {
-      int t = m->joint_type[I.j0 + b], p = m->joint_parent[I.j0 + b];
-      if (t < 0 || t > 3) return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": bad joint type");
-      if (p < 0 || p > b)
-        return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": joint " + std::to_string(b + 1) +
-                                     " has parent " + std::to_string(p) + " (must be < its own number)");
-      if (p != b) I.chain = false;
-      I.nq += joint_nq(t);
-      I.nv += joint_nv(t);
-      sig = (sig ^ (uint64_t)(t * 131 + p)) * 1099511628211ull;
-    }
-    if (I.nv > GPB_MAX_DOF) return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": more than 64 DOF");
-    I.c0 = m->contact_offset ? m->contact_offset[i] : 0;
-    I.nc = m->contact_offset ? m->contact_offset[i + 1] - I.c0 : 0;
-    if (I.nc < 0 || I.nc > GPB_MAX_CONTACTS)
-      return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": contact count outside [0, 64]");
-    for (int k = 0; k < I.nc; ++k) {
-      int bb = m->contact_body[I.c0 + k];
-      if (bb < 1 || bb > I.nb) return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": contact on a missing body");
-    }
-    I.h0 = m->halfspace_offset ? m->halfspace_offset[i] : 0;
-    I.nh = m->halfspace_offset ? m->halfspace_offset[i + 1] - I.h0 : 0;
-    if (I.nh < 0 || I.nh > GPB_MAX_HALFSPACES)
-      return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": half-space count outside [0, 4]");
-    I.model = m->contact_model ? m->contact_model[i] : GPB_HUNT_CROSSLEY;
-    if (I.model != GPB_HUNT_CROSSLEY && I.model != GPB_LINEAR_SPRING_DAMPER)
-      return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": bad contact model");
-    sig = (sig ^ (uint64_t)(I.nc * 7 + I.nh)) * 1099511628211ull;
-    I.sig = sig;
-  }
+  for (int64_t i = 0; i < n; ++i)
+    if (int r = inspect_instance(m, i, &info[i])) return r;
 
   gpb_batch* B = new gpb_batch();
   B->ctx = ctx;
@@ -344,6 +206,23 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
   std::vector<int64_t> qmap(rq * L, -1), vmap(rv * L, -1), cmap(rc * 3 * L, -1);
   std::vector<double> q0(rq * L, 0.0);
   B->status_slot.assign(n, 0);
+  struct VectorSink {  // fill_lane into the host tables below
+    std::vector<uint32_t>* W_;
+    std::vector<double>*TD_, *CD_, *HD_, *Q0_;
+    std::vector<int32_t>*CI_, *LI_;
+    std::vector<int64_t>*QM_, *VM_, *CM_;
+    void li(int64_t i, int32_t x) { (*LI_)[i] = x; }
+    void ci(int64_t i, int32_t x) { (*CI_)[i] = x; }
+    void cd(int64_t i, double x) { (*CD_)[i] = x; }
+    void hd(int64_t i, double x) { (*HD_)[i] = x; }
+    void w(int64_t i, uint32_t x) { (*W_)[i] = x; }
+    void td(int64_t i, double x) { (*TD_)[i] = x; }
+    void q0(int64_t i, double x) { (*Q0_)[i] = x; }
+    void qmap(int64_t i, int64_t x) { (*QM_)[i] = x; }
+    void vmap(int64_t i, int64_t x) { (*VM_)[i] = x; }
+    void cmap(int64_t i, int64_t x) { (*CM_)[i] = x; }
+  } sink{&W, &TD, &CD, &HD, &q0, &CI, &LI, &qmap, &vmap, &cmap};
+
   for (int64_t p = 0; p < npacks; ++p) {
     const PackDesc& P = B->packs_h[p];
     for (int l = 0; l < LANES; ++l) {
@@ -353,91 +232,8 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
         continue;
       }
       const int64_t inst = order[p * LANES + l];
-      const InstInfo& I = info[inst];
       B->status_slot[inst] = (int32_t)(p * LANES + l);
-      LI[li] = (int32_t)inst;
-      LI[li + 1 * L] = I.nb;
-      LI[li + 2 * L] = I.nq;
-      LI[li + 3 * L] = I.nv;
-      LI[li + 4 * L] = I.nc;
-      LI[li + 5 * L] = I.nh;
-      LI[li + 6 * L] = I.model;
-      // contacts sorted by body (stable), remembering the user order
-      std::vector<int> corder(I.nc);
-      std::iota(corder.begin(), corder.end(), 0);
-      std::stable_sort(corder.begin(), corder.end(), [&](int a, int b) {
-        return m->contact_body[I.c0 + a] < m->contact_body[I.c0 + b];
-      });
-      std::vector<int> cfirst(I.nb, 0), ccount(I.nb, 0);
-      for (int k = 0; k < I.nc; ++k) {
-        int src = corder[k];
-        int body = m->contact_body[I.c0 + src] - 1;
-        if (ccount[body] == 0) cfirst[body] = k;
-        ccount[body]++;
-        CI[(P.ctc + k) * L + l] = body | (src << 8);
-        const double* cp = m->contact_params + 6 * (size_t)(I.c0 + src);
-        for (int e = 0; e < CTC_D; ++e) CD[((P.ctc) * CTC_D + CTC_D * k + e) * L + l] = cp[e];
-      }
-      // the kernel writes contact forces by the contact's user-order index
-      for (int k = 0; k < I.nc; ++k)
-        for (int e = 0; e < 3; ++e) cmap[(P.ctc * 3 + 3 * k + e) * L + l] = 3 * (B->c_off[inst] + k) + e;
-      for (int h = 0; h < I.nh; ++h) {
-        const double* hp = m->halfspace_params + 8 * (size_t)(I.h0 + h);
-        double nn = std::sqrt(hp[3] * hp[3] + hp[4] * hp[4] + hp[5] * hp[5]);
-        double vals[8] = {hp[0], hp[1], hp[2], hp[3] / nn, hp[4] / nn, hp[5] / nn, hp[6], hp[7]};
-        for (int e = 0; e < HS_D; ++e) HD[(P.hs * HS_D + HS_D * h + e) * L + l] = vals[e];
-      }
-      // bodies
-      std::vector<bool> branch(I.nb, false);
-      for (int b = 0; b < I.nb; ++b) {
-        int par = m->joint_parent[I.j0 + b];  // 1-based
-        if (par >= 1 && par != b) branch[par - 1] = true;
-      }
-      int qo = 0, vo = 0;
-      for (int b = 0; b < I.nb; ++b) {
-        const int j = I.j0 + b;
-        int t = m->joint_type[j], par = m->joint_parent[j];
-        const double* iso = m->joint_iso + 7 * (size_t)j;
-        const double* ax = m->joint_axis + 3 * (size_t)j;
-        const double* in = m->body_inertia + 10 * (size_t)j;
-        double sk = m->joint_spring ? m->joint_spring[2 * (size_t)j] : 0.0;
-        double sl = m->joint_spring ? m->joint_spring[2 * (size_t)j + 1] : 0.0;
-        uint32_t flags = 0;
-        double R[9];
-        quat_to_rot(iso, R);
-        if (iso[0] == 0.0 && iso[1] == 0.0 && iso[2] == 0.0 && iso[3] == 1.0) flags |= BF_INIT_ROT_IDENTITY;
-        int nz = 0, idx = 0;
-        for (int e = 0; e < 3; ++e)
-          if (ax[e] != 0.0) {
-            nz++;
-            idx = e;
-          }
-        if ((t == GPB_JOINT_REVOLUTE) && nz == 1 && std::fabs(ax[idx]) == 1.0) {
-          flags |= BF_AXIS_PRINCIPAL | ((uint32_t)idx << 2);
-          if (ax[idx] < 0) flags |= BF_AXIS_NEG;
-        }
-        if (branch[b]) flags |= BF_BRANCH;
-        if (t == GPB_JOINT_PRISMATIC && sk != 0.0) flags |= BF_SPRING;
-        if (in[7] == 0.0 && in[8] == 0.0 && in[9] == 0.0) flags |= BF_DIAG_INERTIA;
-        W[((P.topo + b) * 2) * L + l] =
-            (uint32_t)t | ((uint32_t)par << 4) | ((uint32_t)qo << 12) | ((uint32_t)vo << 22);
-        W[((P.topo + b) * 2 + 1) * L + l] =
-            flags | ((uint32_t)cfirst[b] << 8) | ((uint32_t)ccount[b] << 16);
-        double vals[TOPO_D];
-        for (int e = 0; e < 9; ++e) vals[TD_RINIT + e] = R[e];
-        for (int e = 0; e < 3; ++e) vals[TD_TINIT + e] = iso[4 + e];
-        for (int e = 0; e < 3; ++e) vals[TD_AXIS + e] = ax[e];
-        for (int e = 0; e < 10; ++e) vals[TD_INERTIA + e] = in[e];
-        vals[TD_SPRING] = sk;
-        vals[TD_SPRING + 1] = sl;
-        for (int e = 0; e < TOPO_D; ++e) TD[((P.topo) * TOPO_D + TOPO_D * b + e) * L + l] = vals[e];
-        // state maps and the zero state (identity pose for floating joints)
-        for (int e = 0; e < joint_nq(t); ++e) qmap[(P.q + qo + e) * L + l] = B->q_off[inst] + qo + e;
-        if (t == GPB_JOINT_FLOATING) q0[(P.q + qo + 3) * L + l] = 1.0;
-        for (int e = 0; e < joint_nv(t); ++e) vmap[(P.v + vo + e) * L + l] = B->v_off[inst] + vo + e;
-        qo += joint_nq(t);
-        vo += joint_nv(t);
-      }
+      fill_lane(m, inst, info[inst], P, l, (int32_t)inst, B->q_off[inst], B->v_off[inst], B->c_off[inst], sink);
     }
   }
   std::vector<float> TF(TD.begin(), TD.end()), CF(CD.begin(), CD.end()), HF(HD.begin(), HD.end());

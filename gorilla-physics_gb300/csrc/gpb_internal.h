@@ -73,6 +73,24 @@ __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, 
   return s;
 }
 
+// Serving: the job of one lane slot (pack * LANES + lane) of a server's pool.
+// The step kernel runs min(K, steps_left) steps of the slot's request with the
+// request's own step size, integrator and control law, then advances
+// steps_left / step_index.
+struct LaneJob {
+  int64_t steps_left;  // steps still to run (0 = idle slot)
+  int64_t step_index;  // the request's step counter (block index of the open-loop draw)
+  double dt, sigma, kp, kd;
+  uint32_t seed;
+  int32_t control;     // GPB_CONTROL_*
+  int32_t resample;
+  int32_t integrator;
+  int32_t tau_mode;    // host control: 1 = tau_in holds the request's torques
+  int32_t pad;
+};
+constexpr int LANE_JOB_WORDS = (int)(sizeof(LaneJob) / 8);
+static_assert(sizeof(LaneJob) % 8 == 0, "LaneJob is written as 8-byte words");
+
 // Everything a kernel launch needs (device pointers).
 struct DeviceBatch {
   int32_t npacks;
@@ -97,6 +115,25 @@ struct DeviceBatch {
   const int64_t* cmap;     // contact slot (3 per contact) -> flat user index
   int64_t nq_total, nv_total, nc_total;
   int32_t* queue;          // persistent-kernel work counter
+  // serving pool only (all null for a batch)
+  LaneJob* jobs;           // per-slot jobs
+  const int32_t* active;   // packs to run in this launch (nactive of them)
+  int32_t nactive;
+  int32_t* finished;       // slots whose job ended (done or failed) in this launch
+  int32_t* nfinished;
+};
+
+// Scatter of 4- or 8-byte words into up to 16 device arrays: entry k writes
+// bits[k] to element (key[k] & 0xffffffffffff) of target (key[k] >> 56).
+struct ScatterTarget {
+  void* base;
+  int64_t count;  // elements
+  int32_t bytes;  // 4 or 8
+  int32_t pad;
+};
+struct ScatterTable {
+  ScatterTarget t[16];
+  int32_t n;
 };
 
 struct StepParams {
@@ -126,6 +163,11 @@ cudaError_t launch_scatter(const int64_t* map, int64_t slots, const double* src,
                            cudaStream_t s);
 cudaError_t launch_gather(const int64_t* map, int64_t slots, const double* src, double* dst,
                           cudaStream_t s);
+cudaError_t launch_scatter_words(const ScatterTable& table, const uint64_t* key, const uint64_t* bits,
+                                 int64_t n, cudaStream_t s);
+// dst[k] = src[idx[k]] for 4- or 8-byte elements.
+cudaError_t launch_gather_words(const void* src, int bytes, const int64_t* idx, int64_t n, void* dst,
+                                cudaStream_t s);
 // gpb_dynamics_static: the dynamics kernel with its scratch in the library's
 // static device array (cudaErrorInvalidValue if scratch_words exceeds it).
 cudaError_t launch_dynamics_static(const DeviceBatch& b, int device, int64_t scratch_words,

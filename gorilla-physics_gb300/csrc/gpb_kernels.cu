@@ -866,27 +866,51 @@ struct EvalOf<2> {
 template <int PREC>
 __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams p) {
   const int lane = threadIdx.x & 31;
+  const int32_t nwork = b.active ? b.nactive : b.npacks;
   while (true) {
     int pk = 0;
-    if (lane == 0) pk = atomicAdd(b.queue, 1);
+    if (lane == 0) {
+      const int w = atomicAdd(b.queue, 1);
+      pk = w >= nwork ? -1 : (b.active ? b.active[w] : w);
+    }
     pk = __shfl_sync(0xffffffffu, pk, 0);
-    if (pk >= b.npacks) break;
+    if (pk < 0) break;
     const PackDesc pd = b.packs[pk];
     if (lane >= pd.count) continue;
+    const int64_t slot = (int64_t)pk * LANES + lane;
+    // per-slot job of a serving pool: the request's own K, step counter, step
+    // size, integrator and control law
+    StepParams lp = p;
+    int64_t K = p.K;
+    if (b.jobs) {
+      const LaneJob& j = b.jobs[slot];
+      K = j.steps_left < p.K ? j.steps_left : p.K;
+      if (K <= 0) continue;
+      lp.step0 = j.step_index;
+      lp.dt = j.dt;
+      lp.integrator = j.integrator;
+      lp.control = j.control;
+      lp.seed = j.seed;
+      lp.resample = j.resample;
+      lp.sigma = j.sigma;
+      lp.kp = j.kp;
+      lp.kd = j.kd;
+      lp.tau_mode = j.tau_mode;
+    }
     const auto ev = EvalOf<PREC>::make(b, pd, lane);
     const auto& c = ev.c;
-    int32_t* status = b.status + (int64_t)pk * LANES + lane;
+    int32_t* status = b.status + slot;
     const int64_t inst = b.laneI[pd.lane * LANES + lane];
     Col<double> q = col_at(b.q, pd.q, lane), v = col_at(b.v, pd.v, lane);
     Col<double> tin = col_at(b.tau_in, pd.v, lane);
     Col<double> tau{&c.d(c.L.tau)};
     int64_t done = 0;  // steps this instance completed in this launch
-    for (int64_t s = 0; s < p.K; ++s) {
+    for (int64_t s = 0; s < K; ++s) {
       if (*status) break;
-      const int64_t sidx = p.step0 + s;
-      bool ht = control(c, b, p, inst, sidx, s == 0, q, v, tin, tau);
-      Col<double> tsrc = p.control == 0 ? tin : tau;
-      const int st = lane_step(ev, q, v, tsrc, ht, p.dt, p.integrator);
+      const int64_t sidx = lp.step0 + s;
+      bool ht = control(c, b, lp, inst, sidx, s == 0, q, v, tin, tau);
+      Col<double> tsrc = lp.control == 0 ? tin : tau;
+      const int st = lane_step(ev, q, v, tsrc, ht, lp.dt, lp.integrator);
       if (st) {
         *status = st;
         break;
@@ -902,7 +926,13 @@ __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams
         for (int i = 0; i < c.nv; ++i) row[b.nq_total + vm[(size_t)i * LANES]] = v[i];
       }
     }
-    b.done[(int64_t)pk * LANES + lane] = done;
+    b.done[slot] = done;
+    if (b.jobs) {
+      LaneJob& j = b.jobs[slot];
+      j.steps_left -= done;
+      j.step_index += done;
+      if (j.steps_left == 0 || *status) b.finished[atomicAdd(b.nfinished, 1)] = (int32_t)slot;
+    }
   }
 }
 
@@ -945,6 +975,41 @@ __global__ void gather_kernel(const int64_t* map, int64_t slots, const double* s
   }
 }
 
+__global__ void scatter_words_kernel(ScatterTable table, const uint64_t* key, const uint64_t* bits,
+                                     int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint64_t kk = key[k];
+  const int t = (int)(kk >> 56);
+  const int64_t e = (int64_t)(kk & 0xffffffffffffull);
+  if (t >= table.n || e >= table.t[t].count) return;  // the host validates; never write out of bounds
+  if (table.t[t].bytes == 8)
+    reinterpret_cast<uint64_t*>(table.t[t].base)[e] = bits[k];
+  else
+    reinterpret_cast<uint32_t*>(table.t[t].base)[e] = (uint32_t)bits[k];
+}
+cudaError_t launch_scatter_words(const ScatterTable& table, const uint64_t* key, const uint64_t* bits,
+                                 int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  scatter_words_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(table, key, bits, n);
+  return cudaGetLastError();
+}
+template <typename T>
+__global__ void gather_words_kernel(const T* src, const int64_t* idx, int64_t n, T* dst) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = src[idx[k]];
+}
+cudaError_t launch_gather_words(const void* src, int bytes, const int64_t* idx, int64_t n, void* dst,
+                                cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  if (bytes == 8)
+    gather_words_kernel<uint64_t><<<g, 256, 0, s>>>((const uint64_t*)src, idx, n, (uint64_t*)dst);
+  else
+    gather_words_kernel<uint32_t><<<g, 256, 0, s>>>((const uint32_t*)src, idx, n, (uint32_t*)dst);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes_per_instance,
                             int num_sms, int warps_per_sm, cudaStream_t s) {
   (void)lanes_per_instance;
@@ -958,7 +1023,8 @@ cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes
   if (e != cudaSuccess) return e;
   if (warps_per_sm > 0 && warps_per_sm / (threads / 32) < per_sm) per_sm = warps_per_sm / (threads / 32);
   if (per_sm < 1) per_sm = 1;
-  int64_t want = (b.npacks + (threads / 32) - 1) / (threads / 32);
+  const int64_t work = b.active ? b.nactive : b.npacks;
+  int64_t want = (work + (threads / 32) - 1) / (threads / 32);
   int64_t grid = (int64_t)num_sms * per_sm;
   if (grid > want) grid = want;
   if (grid < 1) grid = 1;

@@ -8,6 +8,7 @@ only describes mechanisms and calls the C ABI of include/gpb.h.
 from ._abi import (FIXED, FLOATING, FP64, HUNT_CROSSLEY, LINEAR_SPRING_DAMPER, MIXED, MIXED_REFINED, PRISMATIC,
                    REVOLUTE, RUNGE_KUTTA_2, RUNGE_KUTTA_4, SEMI_IMPLICIT_EULER, GpbError, lib)
 from .batch import Batch, Context, Integrator, Precision, simulate, simulate_steps
+from .serve import Server, SlotClass
 from .model import (WORLD_FRAME, ContactPoint, FixedJoint, FloatingJoint, HalfSpace,
                     MechanismState, Model, PrismaticJoint, RevoluteJoint, RigidBody,
                     SpatialInertia, Transform3D)
@@ -17,5 +18,6 @@ __all__ = [
     "MechanismState", "Transform3D", "SpatialInertia", "RigidBody", "ContactPoint", "HalfSpace",
     "RevoluteJoint", "PrismaticJoint", "FloatingJoint", "FixedJoint", "WORLD_FRAME", "GpbError",
     "lib", "FIXED", "REVOLUTE", "PRISMATIC", "FLOATING", "SEMI_IMPLICIT_EULER", "RUNGE_KUTTA_2",
-    "RUNGE_KUTTA_4", "FP64", "MIXED", "HUNT_CROSSLEY", "LINEAR_SPRING_DAMPER",
+    "RUNGE_KUTTA_4", "FP64", "MIXED", "MIXED_REFINED", "HUNT_CROSSLEY", "LINEAR_SPRING_DAMPER",
+    "Server", "SlotClass",
 ]

@@ -59,6 +59,48 @@ class GpbControl(C.Structure):
     ]
 
 
+class GpbSlotClass(C.Structure):
+    _fields_ = [
+        ("max_bodies", C.c_int32),
+        ("max_q", C.c_int32),
+        ("max_v", C.c_int32),
+        ("max_contacts", C.c_int32),
+        ("max_halfspaces", C.c_int32),
+        ("weight", C.c_double),
+        ("packs", C.c_int32),
+    ]
+
+
+class GpbServerOpts(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int32),
+        ("chunk_steps", C.c_int32),
+        ("hbm_budget_bytes", C.c_int64),
+        ("n_classes", C.c_int32),
+        ("classes", C.POINTER(GpbSlotClass)),
+        ("max_admit_per_tick", C.c_int32),
+    ]
+
+
+class GpbRequest(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double),
+        ("steps", C.c_int64),
+        ("integrator", C.c_int32),
+        ("control", C.c_int32),
+        ("seed", C.c_uint32),
+        ("resample_every", C.c_int32),
+        ("sigma", C.c_double),
+        ("kp", C.c_double),
+        ("kd", C.c_double),
+        ("key", C.c_int32),
+    ]
+
+
+class GpbServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("pending", "active", "completed", "slots", "ticks", "pool_bytes")]
+
+
 # (name, restype, argtypes) of every exported entry point
 SIGNATURES = [
     ("gpb_abi_version", C.c_int, []),
@@ -91,6 +133,15 @@ SIGNATURES = [
     ("gpb_fma_peak", C.c_int, [C.c_int, C.c_int, C.c_int, P_f64]),
     ("gpb_dynamics_static", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                       C.c_void_p, C.c_void_p]),
+    ("gpb_server_plan", C.c_int, [C.POINTER(GpbServerOpts), P_i32, P_i64]),
+    ("gpb_server_create", C.c_int, [C.c_void_p, C.POINTER(GpbServerOpts), C.POINTER(C.c_void_p)]),
+    ("gpb_server_destroy", C.c_int, [C.c_void_p]),
+    ("gpb_server_submit", C.c_int, [C.c_void_p, C.POINTER(GpbModel), C.c_int64, C.c_int64, P_f64, P_f64,
+                                    P_f64, C.POINTER(GpbRequest), C.POINTER(C.c_uint64)]),
+    ("gpb_server_tick", C.c_int, [C.c_void_p, P_i32]),
+    ("gpb_server_completed", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int32, P_i32]),
+    ("gpb_server_result", C.c_int, [C.c_void_p, C.c_uint64, P_f64, P_f64, P_i32, P_i64, P_f64]),
+    ("gpb_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(GpbServerStats)]),
 ]
 GPB_STATIC_SCRATCH_BYTES = 16 << 20
 

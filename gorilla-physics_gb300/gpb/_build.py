@@ -25,7 +25,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 
-SOURCES = ["gpb_kernels.cu", "gpb_host.cpp", "gpb_configs.cpp", "gpb_peaks.cu"]
+SOURCES = ["gpb_kernels.cu", "gpb_host.cpp", "gpb_serve.cpp", "gpb_configs.cpp", "gpb_peaks.cu"]
 
 
 def _compile(src: str, extra: list[str]) -> Path:

@@ -303,6 +303,32 @@ class Model:
                ("joint_offset", "contact_offset", "halfspace_offset")}
         return Model(joint_offset=jo, contact_offset=co, halfspace_offset=ho, **out)
 
+    @classmethod
+    def concat(cls, models: Sequence["Model"]) -> "Model":
+        """The instances of `models`, one after the other."""
+        out = {}
+        for name in ("joint_type", "joint_parent", "joint_iso", "joint_axis", "joint_spring",
+                     "body_inertia", "contact_body", "contact_params", "halfspace_params",
+                     "contact_model"):
+            out[name] = np.concatenate([getattr(m, name)[:cls._used(m, name)] for m in models])
+        for name in ("joint_offset", "contact_offset", "halfspace_offset"):
+            parts, base = [np.zeros(1, np.int64)], 0
+            for m in models:
+                o = getattr(m, name).astype(np.int64)
+                parts.append(o[1:] - o[0] + base)
+                base = int(parts[-1][-1]) if parts[-1].size else base
+            out[name] = np.concatenate(parts)
+        return cls(**out)
+
+    @staticmethod
+    def _used(m: "Model", name: str) -> int:
+        """Length of the used part of a table (struct() may pad empty tables to one entry)."""
+        nj, nc, nh = int(m.joint_offset[-1]), int(m.contact_offset[-1]), int(m.halfspace_offset[-1])
+        per = {"joint_type": nj, "joint_parent": nj, "joint_iso": 7 * nj, "joint_axis": 3 * nj,
+               "joint_spring": 2 * nj, "body_inertia": 10 * nj, "contact_body": nc,
+               "contact_params": 6 * nc, "halfspace_params": 8 * nh, "contact_model": m.n}
+        return per[name]
+
     def struct(self) -> _abi.GpbModel:
         """The ctypes gpb_model pointing at this object's arrays."""
         if self._struct is None:

@@ -306,6 +306,80 @@ int gpb_config_build(int config, int64_t n_instances, uint32_t seed, int contact
 double gpb_open_loop_tau(uint32_t seed, int64_t instance, int64_t block, int32_t dof,
                          double sigma);
 
+/* ---- serving ------------------------------------------------------------ */
+/*
+ * No reference counterpart: the reference steps one MechanismState per call
+ * (src/simulate.rs:20-112).  A server keeps a pool of lane slots resident on
+ * one GPU and runs every admitted request in ticks of at most chunk_steps
+ * steps (continuous batching: requests join and leave between ticks, each
+ * with its own step size, horizon, integrator and control law).  A request's
+ * trajectory does not depend on what else is in the pool: it equals the same
+ * request run alone, bit for bit.
+ *
+ * The pool is divided into slot classes (capacities in bodies, q, v, contacts,
+ * half-spaces).  Each request goes to the smallest class it fits; it waits in
+ * a FIFO queue until that class has a free slot (the admission limit is the
+ * HBM budget the pool was sized to).  A server is single-threaded like its
+ * context.
+ */
+typedef struct gpb_server gpb_server;
+
+typedef struct gpb_slot_class {
+  int32_t max_bodies, max_q, max_v, max_contacts, max_halfspaces;
+  double weight;  /* share of the budget left after the fixed classes; 0 = fixed */
+  int32_t packs;  /* packs of 32 slots of a fixed class (weight 0) */
+} gpb_slot_class;
+
+typedef struct gpb_server_opts {
+  int32_t precision;          /* GPB_FP64, GPB_MIXED or GPB_MIXED_REFINED */
+  int32_t chunk_steps;        /* steps per tick, >= 1 */
+  int64_t hbm_budget_bytes;   /* device bytes of the pool (weighted classes) */
+  int32_t n_classes;          /* 1..16 */
+  const gpb_slot_class* classes;
+  int32_t max_admit_per_tick; /* 0 = no limit */
+} gpb_server_opts;
+
+typedef struct gpb_request {
+  double dt;
+  int64_t steps;            /* horizon K >= 1 */
+  int32_t integrator;       /* GPB_SEMI_IMPLICIT_EULER … */
+  int32_t control;          /* GPB_CONTROL_* */
+  uint32_t seed;            /* open-loop draw seed */
+  int32_t resample_every;
+  double sigma, kp, kd;
+  int32_t key;              /* instance number of the open-loop draw (0 = as a batch of one) */
+} gpb_request;
+
+typedef struct gpb_server_stats {
+  int64_t pending, active, completed, slots, ticks, pool_bytes;
+} gpb_server_stats;
+
+/* Host-only sizing: device bytes of one pack of each class and the packs each
+ * class gets under opts (weighted share of the budget, or its `packs`). */
+int gpb_server_plan(const gpb_server_opts* opts, int32_t* packs_per_class, int64_t* bytes_per_pack);
+int gpb_server_create(gpb_ctx* ctx, const gpb_server_opts* opts, gpb_server** out);
+int gpb_server_destroy(gpb_server* server);
+/* Queues instances first..first+count-1 of m as `count` requests.  q, v (and
+ * tau: host torques for GPB_CONTROL_HOST_TAU, PD targets for GPB_CONTROL_PD,
+ * or NULL) hold those instances' values concatenated in instance order, as
+ * gpb_set_state lays them out.  The server copies everything it needs.
+ * ids receives `count` request ids.  GPB_E_RANGE if an instance fits no class. */
+int gpb_server_submit(gpb_server* server, const gpb_model* m, int64_t first, int64_t count,
+                      const double* q, const double* v, const double* tau,
+                      const gpb_request* requests, uint64_t* ids);
+/* One tick: admit queued requests into free slots, run ≤ chunk_steps steps of
+ * every active request, retire the finished ones.  *completed (nullable) =
+ * requests that finished in this tick. */
+int gpb_server_tick(gpb_server* server, int32_t* completed);
+/* Drains up to `max` ids of finished requests not yet listed. */
+int gpb_server_completed(gpb_server* server, uint64_t* ids, int32_t max, int32_t* count);
+/* Final q, v (nq / nv doubles), status (GPB_ST_* bits), steps run and the
+ * seconds from submission to retirement of a finished request, then forgets
+ * it.  GPB_E_STATE if the request has not finished. */
+int gpb_server_result(gpb_server* server, uint64_t id, double* q, double* v, int32_t* status,
+                      int64_t* steps_done, double* latency_s);
+int gpb_server_stats_get(const gpb_server* server, gpb_server_stats* stats);
+
 /* ---- measurement ------------------------------------------------------- */
 /* FMA throughput of the FP64 (GPB_FP64) or FP32 (GPB_MIXED) pipe in TFLOP/s,
  * counting 2 flops per fused multiply-add of the `active_lanes` (1..32) lanes
