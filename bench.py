@@ -49,6 +49,13 @@ def parse():
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--precision", default="all", choices=["all", "fp64", "mixed", "refined"])
+    ap.add_argument("--serve", action="store_true",
+                    help="serving mix instead: Poisson arrivals, latency percentiles per rate")
+    ap.add_argument("--serve-rates", default="1000,5000,20000", help="arrival rates, requests/s")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window per rate")
+    ap.add_argument("--serve-drain", type=float, default=150.0, help="max seconds to drain after it")
+    ap.add_argument("--serve-precisions", default="mixed,fp64")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM budget of the slot pool")
     return ap.parse_args()
 
 
@@ -377,10 +384,146 @@ def run_gpu(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# serving mix: acrobot / chain / cube / quadruped = 40/30/20/10 %, horizons
+# log-uniform in [100, 50000] steps, Poisson arrivals, continuous batching
+
+SERVE_MIX = (0.4, 0.3, 0.2, 0.1)
+SERVE_HORIZON = (100, 50000)
+
+
+def serve_classes(budget_bytes):
+    """Slot classes of the serving mix (chains split by DOF), budget shares by
+    expected occupancy (mix share × mean per-step cost), and per-class chunk
+    steps that make one tick cost about the same for every class."""
+    from gpb.serve import SlotClass
+
+    def cost(nb, nv, nc):  # algorithmic flops per step (leading terms)
+        return 625 * nb + 11 * nv * (nv + 1) / 2 + nv ** 3 / 3 + 2 * nv * nv + 80 * nc
+
+    specs = [((2, 2, 2, 0, 0), SERVE_MIX[0])]
+    for hi in (8, 16, 24, 32, 40, 48):
+        specs.append(((hi, hi, hi, 0, 0), SERVE_MIX[1] * 8 / 47))
+    specs[-1] = (specs[-1][0], SERVE_MIX[1] * 7 / 47)  # n = 2..48: 47 values
+    specs[1] = (specs[1][0], SERVE_MIX[1] * 7 / 47)
+    specs.append(((1, 7, 6, 8, 1), SERVE_MIX[2]))
+    specs.append(((13, 19, 18, 4, 1), SERVE_MIX[3]))
+    from gpb.serve import plan
+
+    cmax = max(cost(s[0], s[2], s[3]) for s, _ in specs)
+    _, nbytes = plan([SlotClass(*s, packs=1) for s, _ in specs])
+    out = []
+    for (s, share), nb in zip(specs, nbytes):
+        c = cost(s[0], s[2], s[3])
+        # concurrent slots ∝ share × residence time (∝ cost); bytes ∝ slots × pack bytes
+        out.append(SlotClass(*s, weight=share * c * float(nb), chunk_steps=max(1, int(round(16 * cmax / c)))))
+    return out
+
+
+def run_serve(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    import gpb
+    from gpb import Model
+    from gpb.serve import Server
+
+    ctx = gpb.Context(0)
+    prec_of = {"fp64": gpb.FP64, "mixed": gpb.MIXED, "refined": gpb.MIXED_REFINED}
+    runs = []
+    for pname in args.serve_precisions.split(","):
+        for rate in [float(r) for r in args.serve_rates.split(",")]:
+            rng = np.random.default_rng(args.seed)
+            n = int(rng.poisson(rate * args.serve_seconds))
+            t_arr = np.sort(rng.uniform(0.0, args.serve_seconds, n))
+            cfg = rng.choice(4, size=n, p=SERVE_MIX)
+            lo, hi = np.log(SERVE_HORIZON[0]), np.log(SERVE_HORIZON[1])
+            horizon = np.exp(rng.uniform(lo, hi, n)).astype(np.int64)
+            per = []
+            for c in range(4):
+                idx = np.nonzero(cfg == c)[0]
+                M, q0, v0, aux = Model.from_config(c, max(len(idx), 1), seed=args.seed + 17 * c)
+                per.append({"idx": idx, "M": M, "q0": q0, "v0": v0, "aux": aux, "next": 0,
+                            "t": t_arr[idx]})
+            S = Server(ctx, serve_classes(int(args.serve_budget_gb * 1e9)), precision=prec_of[pname],
+                       chunk_steps=16, hbm_budget_bytes=int(args.serve_budget_gb * 1e9))
+            req_of = {}
+            lat = np.full(n, np.nan)
+            steps_done_total = 0
+            ticks = 0
+            tick_s = []
+            t0 = time.perf_counter()
+            deadline = args.serve_seconds + args.serve_drain
+            while True:
+                now = time.perf_counter() - t0
+                for c, P in enumerate(per):
+                    upto = int(np.searchsorted(P["t"], now, side="right"))
+                    if upto > P["next"]:
+                        a, b = P["next"], upto
+                        ids = S.submit(P["M"], a, b - a, P["q0"], P["v0"], dt=DT[c],
+                                       steps=horizon[P["idx"][a:b]], control=CONTROL[c],
+                                       tau=P["aux"] if c == 3 else None, seed=7 + c, kp=50.0,
+                                       kd=2.0, keys=0)
+                        for rid, r in zip(ids.tolist(), P["idx"][a:b].tolist()):
+                            req_of[rid] = r
+                        P["next"] = b
+                st = S.stats()
+                all_in = all(P["next"] == len(P["idx"]) for P in per)
+                if all_in and st["pending"] == 0 and st["active"] == 0:
+                    break
+                if now > deadline:
+                    break
+                if st["pending"] == 0 and st["active"] == 0:
+                    continue  # idle until the next arrival
+                ts = time.perf_counter()
+                S.tick()
+                ticks += 1
+                tick_s.append(time.perf_counter() - ts)
+                done = S.completed()
+                if done.size:
+                    tdone = time.perf_counter() - t0
+                    for rid in done.tolist():
+                        r = req_of.pop(rid)
+                        lat[r] = tdone - t_arr[r]
+                        steps_done_total += int(horizon[r])
+                    S.forget(done)
+            wall = time.perf_counter() - t0
+            ok = np.isfinite(lat)
+            offered = float(rate * np.mean(horizon)) if n else 0.0
+            runs.append({
+                "precision": pname, "rate_req_s": rate, "requests": n, "completed": int(ok.sum()),
+                "censored": int((~ok).sum()),
+                "latency_s": {"p50": float(np.quantile(lat[ok], 0.5)) if ok.any() else None,
+                              "p99": float(np.quantile(lat[ok], 0.99)) if ok.any() else None,
+                              "max": float(lat[ok].max()) if ok.any() else None},
+                "latency_by_config_p50_s": {CONFIG_NAME[c]: float(np.median(lat[ok & (cfg == c)]))
+                                            for c in range(4) if (ok & (cfg == c)).any()},
+                "offered_instance_steps_per_s": offered,
+                "achieved_instance_steps_per_s": steps_done_total / wall,
+                "wall_s": wall, "ticks": ticks,
+                "tick_ms": {"p50": 1e3 * float(np.median(tick_s)) if tick_s else None,
+                            "p99": 1e3 * float(np.quantile(tick_s, 0.99)) if tick_s else None},
+                "pool_bytes": S.stats()["pool_bytes"]})
+            S.close()
+            print(json.dumps(runs[-1]), file=sys.stderr, flush=True)
+    line = {"metric": "serving latency (p50/p99) and throughput, Poisson arrivals",
+            "unit": "s", "n_gpus": 1, "higher_is_better": False,
+            "config": {"workload": "serving mix acrobot/chain/cube/quadruped = 40/30/20/10 %",
+                       "horizon_steps": "log-uniform [100, 50000]",
+                       "arrival_window_s": args.serve_seconds, "hbm_budget_gb": args.serve_budget_gb,
+                       "admission": "FIFO per slot class; pool sized to the budget"},
+            "data": "synthetic (seeded)", "runs": runs}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.serve:
+        return run_serve(args)
     return run_gpu(args)
 
 

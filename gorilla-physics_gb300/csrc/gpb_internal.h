@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 namespace gpb {
@@ -78,18 +79,19 @@ __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, 
 // request's own step size, integrator and control law, then advances
 // steps_left / step_index.
 struct LaneJob {
-  int64_t steps_left;  // steps still to run (0 = idle slot)
-  int64_t step_index;  // the request's step counter (block index of the open-loop draw)
+  int64_t steps_left;  // steps still to run (0 = idle slot, or a job that failed)
+  int64_t step_index;  // steps the request has run (its step counter for the open-loop draw)
   double dt, sigma, kp, kd;
   uint32_t seed;
   int32_t control;     // GPB_CONTROL_*
   int32_t resample;
   int32_t integrator;
   int32_t tau_mode;    // host control: 1 = tau_in holds the request's torques
-  int32_t pad;
+  int32_t chunk;       // steps per launch of this slot (0 = the launch's K)
 };
 constexpr int LANE_JOB_WORDS = (int)(sizeof(LaneJob) / 8);
 static_assert(sizeof(LaneJob) % 8 == 0, "LaneJob is written as 8-byte words");
+static_assert(offsetof(LaneJob, step_index) == 8, "the server gathers step_index as word 1");
 
 // Everything a kernel launch needs (device pointers).
 struct DeviceBatch {

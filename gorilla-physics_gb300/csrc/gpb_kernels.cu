@@ -884,7 +884,8 @@ __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams
     int64_t K = p.K;
     if (b.jobs) {
       const LaneJob& j = b.jobs[slot];
-      K = j.steps_left < p.K ? j.steps_left : p.K;
+      const int64_t kc = j.chunk > 0 ? j.chunk : p.K;
+      K = j.steps_left < kc ? j.steps_left : kc;
       if (K <= 0) continue;
       lp.step0 = j.step_index;
       lp.dt = j.dt;
@@ -931,7 +932,8 @@ __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams
       LaneJob& j = b.jobs[slot];
       j.steps_left -= done;
       j.step_index += done;
-      if (j.steps_left == 0 || *status) b.finished[atomicAdd(b.nfinished, 1)] = (int32_t)slot;
+      if (*status) j.steps_left = 0;  // a failed job ends here (step_index = steps run)
+      if (j.steps_left == 0) b.finished[atomicAdd(b.nfinished, 1)] = (int32_t)slot;
     }
   }
 }

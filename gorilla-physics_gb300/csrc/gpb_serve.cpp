@@ -45,6 +45,7 @@ enum Target { T_W, T_TD, T_TF, T_CI, T_CD, T_CF, T_HD, T_HF, T_LI, T_Q, T_V, T_T
 struct ClassInfo {
   gpb_slot_class caps;
   int32_t first_pack = 0, npacks = 0;
+  int32_t high = 0;  // packs [first_pack, first_pack + high) have held a request
   int64_t pack_bytes = 0;
   std::vector<int32_t> free_slots;  // stack
 };
@@ -113,7 +114,8 @@ int64_t pack_bytes(const gpb_slot_class& c) {
 int check_class(const gpb_slot_class& c) {
   if (c.max_bodies < 1 || c.max_bodies > GPB_MAX_BODIES || c.max_q < 0 || c.max_q > 7 * GPB_MAX_BODIES ||
       c.max_v < 0 || c.max_v > GPB_MAX_DOF || c.max_contacts < 0 || c.max_contacts > GPB_MAX_CONTACTS ||
-      c.max_halfspaces < 0 || c.max_halfspaces > GPB_MAX_HALFSPACES || c.weight < 0.0 || c.packs < 0)
+      c.max_halfspaces < 0 || c.max_halfspaces > GPB_MAX_HALFSPACES || c.weight < 0.0 || c.packs < 0 ||
+      c.chunk_steps < 0)
     return fail(GPB_E_RANGE, "gpb_server: slot class capacity outside the documented limits");
   return GPB_OK;
 }
@@ -531,11 +533,13 @@ extern "C" int gpb_server_tick(gpb_server* S, int32_t* completed_now) {
     j.resample = R.req.resample_every > 0 ? R.req.resample_every : 1;
     j.integrator = R.req.integrator;
     j.tau_mode = (R.req.control == GPB_CONTROL_HOST_TAU && !R.tau.empty()) ? 1 : 0;
+    j.chunk = C.caps.chunk_steps;
     uint64_t words[LANE_JOB_WORDS];
     std::memcpy(words, &j, sizeof(j));
     for (int w = 0; w < LANE_JOB_WORDS; ++w) sink.put(T_JOBS, (int64_t)slot * LANE_JOB_WORDS + w, words[w]);
     S->slot_req[slot] = R.id;
     S->pack_active[pk]++;
+    C.high = std::max(C.high, pk - C.first_pack + 1);
     S->running.emplace(R.id, std::move(R));
     it = S->pending.erase(it);
     ++admitted;
@@ -560,7 +564,7 @@ extern "C" int gpb_server_tick(gpb_server* S, int32_t* completed_now) {
   std::vector<int32_t> act;
   for (int c : S->class_order) {
     const ClassInfo& C = S->classes[c];
-    for (int32_t p = C.first_pack; p < C.first_pack + C.npacks; ++p)
+    for (int32_t p = C.first_pack; p < C.first_pack + C.high; ++p)  // slots are taken lowest first
       if (S->pack_active[p] > 0) act.push_back(p);
   }
   S->ticks++;
@@ -595,13 +599,19 @@ extern "C" int gpb_server_tick(gpb_server* S, int32_t* completed_now) {
   CUDA_TRY(cudaStreamSynchronize(s));
   // ---- retirement: gather q, v, steps left and status of the finished slots --
   std::vector<int64_t> qi, vi, ji, si;
+  // a slot is listed once per job end: its job is then idle until a new admission
+  std::vector<int32_t> keep;
+  keep.reserve(fin.size());
+  for (int32_t slot : fin)
+    if (slot >= 0 && (size_t)slot < S->slot_req.size() && S->running.count(S->slot_req[slot])) keep.push_back(slot);
+  if (keep.size() != fin.size()) return fail(GPB_E_CUDA, "gpb_server_tick: finished list names an idle slot");
   for (int32_t slot : fin) {
     const int32_t pk = slot / LANES, l = slot % LANES;
     const PackDesc& P = S->pool.packs_h[pk];
     const Request& R = S->running.at(S->slot_req[slot]);
     for (int e = 0; e < R.info.nq; ++e) qi.push_back((P.q + e) * L + l);
     for (int e = 0; e < R.info.nv; ++e) vi.push_back((P.v + e) * L + l);
-    ji.push_back((int64_t)slot * LANE_JOB_WORDS);  // steps_left is word 0 of LaneJob
+    ji.push_back((int64_t)slot * LANE_JOB_WORDS + 1);  // step_index (steps run) is word 1 of LaneJob
     si.push_back(slot);
   }
   const size_t nidx = qi.size() + vi.size() + ji.size() + si.size();
@@ -643,9 +653,7 @@ extern "C" int gpb_server_tick(gpb_server* S, int32_t* completed_now) {
     std::memcpy(res.v.data(), outw.data() + ov, R.info.nv * 8);
     oq += R.info.nq;
     ov += R.info.nv;
-    int64_t left;
-    std::memcpy(&left, outw.data() + oj + k, 8);
-    res.steps_done = R.req.steps - left;
+    std::memcpy(&res.steps_done, outw.data() + oj + k, 8);
     res.status = (int32_t)st32[k];
     res.latency_s = std::chrono::duration<double>(now - R.t_submit).count();
     S->results.emplace(id, std::move(res));
@@ -683,6 +691,12 @@ extern "C" int gpb_server_result(gpb_server* S, uint64_t id, double* q, double* 
   if (steps_done) *steps_done = r.steps_done;
   if (latency_s) *latency_s = r.latency_s;
   S->results.erase(it);
+  return GPB_OK;
+}
+
+extern "C" int gpb_server_forget(gpb_server* S, const uint64_t* ids, int64_t count) {
+  if (!S || (count > 0 && !ids)) return fail(GPB_E_INVAL, "gpb_server_forget: NULL argument");
+  for (int64_t k = 0; k < count; ++k) S->results.erase(ids[k]);
   return GPB_OK;
 }
 

@@ -68,6 +68,7 @@ class GpbSlotClass(C.Structure):
         ("max_halfspaces", C.c_int32),
         ("weight", C.c_double),
         ("packs", C.c_int32),
+        ("chunk_steps", C.c_int32),
     ]
 
 
@@ -141,6 +142,7 @@ SIGNATURES = [
     ("gpb_server_tick", C.c_int, [C.c_void_p, P_i32]),
     ("gpb_server_completed", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int32, P_i32]),
     ("gpb_server_result", C.c_int, [C.c_void_p, C.c_uint64, P_f64, P_f64, P_i32, P_i64, P_f64]),
+    ("gpb_server_forget", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int64]),
     ("gpb_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(GpbServerStats)]),
 ]
 GPB_STATIC_SCRATCH_BYTES = 16 << 20

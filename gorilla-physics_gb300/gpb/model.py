@@ -269,6 +269,11 @@ class Model:
 
     def offsets(self):
         """Per-instance flattened q / v / contact offsets ([n+1] each)."""
+        if getattr(self, "_offsets", None) is None:
+            self._offsets = self._compute_offsets()
+        return self._offsets
+
+    def _compute_offsets(self):
         t = self.joint_type
         nqj = np.choose(t, [0, 1, 1, 7])
         nvj = np.choose(t, [0, 1, 1, 6])

@@ -30,10 +30,19 @@ class SlotClass:
     max_halfspaces: int = 0
     weight: float = 0.0  # share of hbm_budget_bytes (0: use `packs`)
     packs: int = 0       # packs of 32 slots
+    chunk_steps: int = 0  # steps per tick of this class (0: the server's chunk_steps)
 
     def struct(self) -> _abi.GpbSlotClass:
         return _abi.GpbSlotClass(self.max_bodies, self.max_q, self.max_v, self.max_contacts,
-                                 self.max_halfspaces, float(self.weight), int(self.packs))
+                                 self.max_halfspaces, float(self.weight), int(self.packs),
+                                 int(self.chunk_steps))
+
+
+# numpy image of gpb_request (same field order and alignment)
+REQUEST_DTYPE = np.dtype([("dt", "f8"), ("steps", "i8"), ("integrator", "i4"), ("control", "i4"),
+                          ("seed", "u4"), ("resample_every", "i4"), ("sigma", "f8"), ("kp", "f8"),
+                          ("kd", "f8"), ("key", "i4")], align=True)
+assert REQUEST_DTYPE.itemsize == C.sizeof(_abi.GpbRequest)
 
 
 def _opts(classes, precision, chunk_steps, hbm_budget_bytes, max_admit_per_tick):
@@ -99,13 +108,15 @@ class Server:
         bc = lambda x, t: np.broadcast_to(np.asarray(x, t), (count,))
         dts, ks, seeds = bc(dt, np.float64), bc(steps, np.int64), bc(seed, np.uint32)
         keys = bc(0 if keys is None else keys, np.int32)
-        reqs = (_abi.GpbRequest * max(count, 1))()
-        for k in range(count):
-            reqs[k] = _abi.GpbRequest(float(dts[k]), int(ks[k]), integrator, mode, int(seeds[k]),
-                                      resample_every, sigma, kp, kd, int(keys[k]))
+        reqs = np.zeros(max(count, 1), REQUEST_DTYPE)
+        reqs["dt"][:count], reqs["steps"][:count], reqs["seed"][:count] = dts, ks, seeds
+        reqs["key"][:count] = keys
+        reqs["integrator"], reqs["control"], reqs["resample_every"] = integrator, mode, resample_every
+        reqs["sigma"], reqs["kp"], reqs["kd"] = sigma, kp, kd
         ids = np.zeros(max(count, 1), np.uint64)
         _abi.check(_abi.lib().gpb_server_submit(
-            self.h, C.byref(model.struct()), first, count, _p(qs), _p(vs), _p(ts), reqs,
+            self.h, C.byref(model.struct()), first, count, _p(qs), _p(vs), _p(ts),
+            reqs.ctypes.data_as(C.POINTER(_abi.GpbRequest)),
             ids.ctypes.data_as(C.POINTER(C.c_uint64))), "gpb_server_submit")
         ids = ids[:count]
         nq = np.diff(qo)[first:first + count]
@@ -130,7 +141,7 @@ class Server:
 
     def result(self, rid: int):
         """(q, v, status, steps_done, latency_s) of a finished request (then forgotten)."""
-        nq, nv = self._dims.pop(int(rid))
+        nq, nv = self._dims.get(int(rid), (0, 0))  # unknown ids: the library reports the error
         q = np.zeros(max(nq, 1))
         v = np.zeros(max(nv, 1))
         st = C.c_int32()
@@ -138,7 +149,16 @@ class Server:
         lat = C.c_double()
         _abi.check(_abi.lib().gpb_server_result(self.h, C.c_uint64(int(rid)), _p(q), _p(v), C.byref(st),
                                                 C.byref(sd), C.byref(lat)), "gpb_server_result")
+        self._dims.pop(int(rid), None)
         return q[:nq], v[:nv], st.value, sd.value, lat.value
+
+    def forget(self, ids) -> None:
+        """Drops the results of finished requests without reading them."""
+        ids = np.ascontiguousarray(ids, np.uint64)
+        for i in ids.tolist():
+            self._dims.pop(i, None)
+        _abi.check(_abi.lib().gpb_server_forget(self.h, ids.ctypes.data_as(C.POINTER(C.c_uint64)), ids.size),
+                   "gpb_server_forget")
 
     def stats(self) -> dict:
         s = _abi.GpbServerStats()

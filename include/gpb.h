@@ -328,6 +328,7 @@ typedef struct gpb_slot_class {
   int32_t max_bodies, max_q, max_v, max_contacts, max_halfspaces;
   double weight;  /* share of the budget left after the fixed classes; 0 = fixed */
   int32_t packs;  /* packs of 32 slots of a fixed class (weight 0) */
+  int32_t chunk_steps; /* steps per tick of this class's requests (0 = the server's) */
 } gpb_slot_class;
 
 typedef struct gpb_server_opts {
@@ -378,6 +379,8 @@ int gpb_server_completed(gpb_server* server, uint64_t* ids, int32_t max, int32_t
  * it.  GPB_E_STATE if the request has not finished. */
 int gpb_server_result(gpb_server* server, uint64_t id, double* q, double* v, int32_t* status,
                       int64_t* steps_done, double* latency_s);
+/* Forgets the results of finished requests without reading them. */
+int gpb_server_forget(gpb_server* server, const uint64_t* ids, int64_t count);
 int gpb_server_stats_get(const gpb_server* server, gpb_server_stats* stats);
 
 /* ---- measurement ------------------------------------------------------- */
