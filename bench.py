@@ -59,6 +59,23 @@ def parse():
     return ap.parse_args()
 
 
+def shard_seed(seed: int, rank: int) -> int:
+    """Each rank steps its own instances (weak scaling: no data-path collective)."""
+    return seed + 1000 * rank
+
+
+def all_reduce(x: float, op: str, world: int, device: str) -> float:
+    """Max or sum of a per-rank scalar (timings: max over ranks; work: sum)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -233,7 +250,7 @@ def run_gpu(args):
     L = gpb.lib()
     ctx = gpb.Context(local)
     # weak scaling: every rank owns its own instances (seed offset by rank)
-    M, q0, v0, aux = Model.from_config(args.config, args.instances, seed=args.seed + 1000 * rank)
+    M, q0, v0, aux = Model.from_config(args.config, args.instances, seed=shard_seed(args.seed, rank))
     B = Batch(M, ctx)
     flops_step = float(model_flops(M, 0).sum())
     kw = dict(control=CONTROL[args.config], tau=aux if args.config == 3 else None, seed=7,
@@ -245,18 +262,10 @@ def run_gpu(args):
             torch.distributed.barrier()
 
     def reduce_max(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return all_reduce(x, "max", world, f"cuda:{local}")
 
     def reduce_sum(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        return float(t.item())
+        return all_reduce(x, "sum", world, f"cuda:{local}")
 
     inst_flops = model_flops(M, 0).astype(np.float64)
 
@@ -264,10 +273,14 @@ def run_gpu(args):
     precs = {"all": ["fp64", "mixed", "refined"], "fp64": ["fp64"], "mixed": ["mixed"],
              "refined": ["refined"]}[args.precision]
     PREC = {"fp64": gpb.FP64, "mixed": gpb.MIXED, "refined": gpb.MIXED_REFINED}
+    launch = {}
     for name in precs:
         prec = PREC[name]
         B.update(q0, v0)
         B.clear_status()
+        # launch shape for this workload and precision (short trials, state restored)
+        w, c = B.autotune(dt, 0, prec, trial_steps=10, **kw)
+        launch[name] = {"warps_per_sm": w, "coop_min_dof": c}
         if args.warmup:
             B.simulate_steps(args.warmup, dt, 0, prec, step0=0, **kw)
         barrier()
@@ -359,6 +372,7 @@ def run_gpu(args):
         line["modes"][name] = {
             "value": r["done"] / (r["kernel_ms"] * 1e-3), "ms_per_step": r["kernel_ms"] / args.steps,
             "roofline": roof(r, *bound[name]),
+            "launch": launch.get(name),
             "qdd_rel_err_vs_fp64": errs.get(name)}
     if "fp64" in results:
         line["fp64"] = line["modes"]["fp64"]

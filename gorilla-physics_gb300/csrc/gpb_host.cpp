@@ -175,6 +175,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
     std::memset(&P, 0, sizeof(P));
     P.count = (int32_t)std::min<int64_t>(LANES, n - p * LANES);
     P.chain = 1;
+    P.minnv = GPB_MAX_DOF;
     for (int l = 0; l < P.count; ++l) {
       const InstInfo& I = info[order[p * LANES + l]];
       P.nb = std::max(P.nb, I.nb);
@@ -182,6 +183,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
       P.nv = std::max(P.nv, I.nv);
       P.nc = std::max(P.nc, I.nc);
       P.nh = std::max(P.nh, I.nh);
+      P.minnv = std::min(P.minnv, I.nv);
       if (!I.chain) P.chain = 0;
     }
     P.topo = rt;
@@ -269,7 +271,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
   chk(B->stage_q.alloc(std::max<int64_t>(B->nq_total, 1)));
   chk(B->stage_v.alloc(std::max<int64_t>(B->nv_total, 1)));
   chk(B->stage_c.alloc(std::max<int64_t>(3 * B->nc_total, 1)));
-  chk(B->queue.alloc(1));
+  chk(B->queue.alloc(2));
   if (e != cudaSuccess) {
     B->release();
     delete B;
@@ -328,6 +330,26 @@ extern "C" int gpb_batch_set_mapping(gpb_batch* b, int lanes) {
   if (lanes != 0 && lanes != 1) return fail(GPB_E_INVAL, "gpb_batch_set_mapping: lanes must be 0 or 1");
   b->mapping = lanes;
   return GPB_OK;
+}
+
+extern "C" int gpb_batch_set_coop(gpb_batch* b, int min_dof) {
+  if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_coop: batch is NULL");
+  if (min_dof < -1 || min_dof > GPB_MAX_DOF)
+    return fail(GPB_E_INVAL, "gpb_batch_set_coop: min_dof must be -1 (default), 0 (off) or 1..64");
+  b->coop_min_dof = min_dof;
+  return GPB_OK;
+}
+
+// Packs at the front of the queue whose every instance has at least the
+// block-cooperative threshold of DOF (packs are sorted by DOF, largest first).
+static int32_t coop_packs(const gpb_batch* b, int precision) {
+  if (precision == GPB_MIXED_REFINED) return 0;
+  int thr = b->coop_min_dof < 0 ? kDefaultCoopMinDof : b->coop_min_dof;
+  if (thr <= 0) return 0;
+  if (precision == GPB_MIXED) thr = std::max(thr, 13);  // the FP64-factor form of GPB_MIXED
+  int32_t n = 0;
+  while (n < b->npacks && b->packs_h[n].minnv >= thr) ++n;
+  return n;
 }
 
 extern "C" int gpb_batch_set_launch(gpb_batch* b, int warps_per_sm) {
@@ -456,6 +478,7 @@ static int run_simulate(gpb_batch* b, double dt, int64_t K, int64_t step0, int i
     p.history = b->hist.p;
     p.record_every = record_every;
   }
+  p.ncoop = coop_packs(b, precision);
   if (b->npacks > 0 && K > 0) {
     CUDA_TRY(cudaEventRecord(b->ctx->ev0, s));
     CUDA_TRY(launch_simulate(b->dev(), p, b->mapping, b->ctx->num_sms, b->warps_per_sm, s));
@@ -478,6 +501,69 @@ extern "C" int gpb_step(gpb_batch* b, double dt, const double* tau, int integrat
   int r = run_simulate(b, dt, 1, 0, integrator, precision, &c, 0, nullptr);
   if (r) return r;
   CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
+  return GPB_OK;
+}
+
+// Launch-shape autotuner: short timed trials of the batch's own step from its
+// current state (restored after every trial and at the end).
+extern "C" int gpb_batch_autotune(gpb_batch* b, double dt, int integrator, int precision,
+                                  const gpb_control_params* control, int trial_steps, int* warps_per_sm,
+                                  int* coop_min_dof) {
+  if (!b) return fail(GPB_E_INVAL, "gpb_batch_autotune: batch is NULL");
+  if (int r = check_enums(integrator, precision)) return r;
+  if (trial_steps < 1) return fail(GPB_E_INVAL, "gpb_batch_autotune: trial_steps must be >= 1");
+  CUDA_TRY(cudaSetDevice(b->ctx->device));
+  cudaStream_t s = b->ctx->stream;
+  DBuf<double> q0, v0, t0;
+  DBuf<int32_t> st0;
+  CUDA_TRY(q0.alloc(b->q.n));
+  CUDA_TRY(v0.alloc(b->v.n));
+  CUDA_TRY(t0.alloc(b->tau_in.n));
+  CUDA_TRY(st0.alloc(b->status.n));
+  auto copy = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s) : cudaSuccess;
+  };
+  auto save_restore = [&](bool save) -> cudaError_t {
+    cudaError_t e = save ? copy(q0.p, b->q.p, b->q.n * 8) : copy(b->q.p, q0.p, b->q.n * 8);
+    if (e == cudaSuccess) e = save ? copy(v0.p, b->v.p, b->v.n * 8) : copy(b->v.p, v0.p, b->v.n * 8);
+    if (e == cudaSuccess)
+      e = save ? copy(t0.p, b->tau_in.p, b->tau_in.n * 8) : copy(b->tau_in.p, t0.p, b->tau_in.n * 8);
+    if (e == cudaSuccess)
+      e = save ? copy(st0.p, b->status.p, b->status.n * 4) : copy(b->status.p, st0.p, b->status.n * 4);
+    return e;
+  };
+  CUDA_TRY(save_restore(true));
+  const int keep_w = b->warps_per_sm, keep_c = b->coop_min_dof;
+  std::vector<std::pair<int, int>> cand;
+  for (int w : {4, 8}) {
+    cand.push_back({w, 0});
+    if (precision != GPB_MIXED_REFINED && b->npacks > 0 && b->packs_h[0].minnv >= 32)
+      for (int c : {40, 32}) cand.push_back({w, c});
+  }
+  double best = 1e300;
+  std::pair<int, int> pick{keep_w, keep_c};
+  int err = GPB_OK;
+  for (const auto& cw : cand) {
+    b->warps_per_sm = cw.first;
+    b->coop_min_dof = cw.second;
+    CUDA_TRY(save_restore(false));
+    // one untimed step, then the timed trial
+    err = run_simulate(b, dt, 1, 0, integrator, precision, control, 0, nullptr);
+    if (err == GPB_OK) err = run_simulate(b, dt, trial_steps, 1, integrator, precision, control, 0, nullptr);
+    if (err != GPB_OK) break;
+    const double ms = gpb_last_launch_ms(b->ctx);
+    if (ms >= 0.0 && ms < best) {
+      best = ms;
+      pick = cw;
+    }
+  }
+  b->warps_per_sm = err == GPB_OK ? pick.first : keep_w;
+  b->coop_min_dof = err == GPB_OK ? pick.second : keep_c;
+  CUDA_TRY(save_restore(false));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (err != GPB_OK) return err;
+  if (warps_per_sm) *warps_per_sm = pick.first;
+  if (coop_min_dof) *coop_min_dof = pick.second;
   return GPB_OK;
 }
 

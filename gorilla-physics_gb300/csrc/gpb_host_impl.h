@@ -18,6 +18,9 @@
 
 namespace gpb {
 
+// Default DOF threshold of the block-cooperative packs (gpb_batch_set_coop).
+constexpr int kDefaultCoopMinDof = 0;
+
 // Records `msg` as the calling thread's last error and returns `code`.
 int fail(int code, const std::string& msg);
 
@@ -194,6 +197,7 @@ struct gpb_batch {
   int32_t npacks = 0;
   int mapping = 0;
   int warps_per_sm = 0;  // resident warps per SM of the step kernel (0 = occupancy limit)
+  int coop_min_dof = -1; // block-cooperative packs: DOF threshold (-1 = default, 0 = off)
   std::vector<int64_t> q_off, v_off, c_off;  // user layout, [n+1]
   int64_t nq_total = 0, nv_total = 0, nc_total = 0;
   std::vector<gpb::PackDesc> packs_h;

@@ -34,7 +34,7 @@ constexpr int HS_D = 8;     // point (3), normal (3), alpha, mu
 constexpr int LANE_I = 8;   // per-lane ints: instance, nb, nq, nv, nc, nh, contact model, pad
 
 struct PackDesc {
-  int32_t count, nb, nq, nv, nc, nh, chain, pad;
+  int32_t count, nb, nq, nv, nc, nh, chain, minnv;  // minnv: smallest DOF count of its lanes
   // bases in rows (one row = LANES elements)
   int64_t topo;   // topology bodies (2 int words / TOPO_D reals per body)
   int64_t ctc;    // contacts
@@ -116,7 +116,7 @@ struct DeviceBatch {
   const int64_t* vmap;
   const int64_t* cmap;     // contact slot (3 per contact) -> flat user index
   int64_t nq_total, nv_total, nc_total;
-  int32_t* queue;          // persistent-kernel work counter
+  int32_t* queue;          // persistent-kernel work counters: [0] per-warp packs, [1] block packs
   // serving pool only (all null for a batch)
   LaneJob* jobs;           // per-slot jobs
   const int32_t* active;   // packs to run in this launch (nactive of them)
@@ -153,6 +153,7 @@ struct StepParams {
   double* qdd_out;      // dynamics-only: user-order q̈ (device)
   double* cforce_out;   // dynamics-only: user-order contact forces (device)
   int32_t tau_mode;     // dynamics/step: 0 = zero torque, 1 = tau_in holds torques
+  int32_t ncoop;        // packs [0, ncoop) are stepped by a whole 4-warp block
 };
 
 // Launchers (gpb_kernels.cu).  All return a cudaError_t.

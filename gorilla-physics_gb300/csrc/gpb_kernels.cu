@@ -201,97 +201,131 @@ __device__ __forceinline__ R sdot2(const SV<R>& a, const SV<R>& b) {
 template <typename R, typename RC>
 __device__ __noinline__ void lane_solve(const LaneCtx<R>& c);
 
-// Cholesky H = L Lᵀ (left-looking, 4×4 register tiles: every tile update is 16
-// independent multiply-add chains over 32 loaded words — 2 FMAs per load) and
-// the solves L y = rhs, Lᵀ x = y.  n is padded to a multiple of 4 with identity
-// rows.  Writes q̈ into `qdd`; returns GPB status bits.
+// Diagonal tile J of the left-looking Cholesky H = L Lᵀ: a = A_JJ − Σ_K L_JK
+// L_JKᵀ (4×4 register tiles: 16 independent multiply-add chains over 16 loaded
+// words), then its own 4×4 factor into tile (J, J) and the reciprocal
+// diagonal into D.  Returns GPB_ST_CHOL_FAIL for a non-positive pivot.  Not
+// inlined: the one-warp and block-cooperative factorisations call this one
+// compiled function, so both round identically.
 template <typename R, typename RC>
-__device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& cin, Col<double> qdd) {
-  const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
-  const int nv = c.nv, nT = (nv + 3) >> 2, np = nT << 2;
+__device__ __noinline__ int chol_diag(const LaneCtx<R>& cin, int J) {
+  const LaneCtx<R> c = cin;
   const int M = c.L.M;
-  for (int i = nv; i < np; ++i) {
-    for (int j = 0; j < i; ++j) c.template x<RC>(M + tix(i, j)) = RC(0);
-    c.template x<RC>(M + tix(i, i)) = RC(1);
-    c.template x<RC>(c.L.rhs + i) = RC(0);
-  }
-  int st = 0;
-  for (int J = 0; J < nT; ++J) {
-    const int tJJ = M + tile(J, J);
-    RC a[4][4];
+  const int tJJ = M + tile(J, J);
+  RC a[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int s = 0; s <= r; ++s) a[r][s] = (c.template x<RC>(tJJ + 4 * r + s));
+  for (int K = 0; K < J; ++K) {
+    const int tJK = M + tile(J, K);
+    RC l[4][4];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) l[e >> 2][e & 3] = (c.template x<RC>(tJK + e));
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
-      for (int s = 0; s <= r; ++s) a[r][s] = (c.template x<RC>(tJJ + 4 * r + s));
-    for (int K = 0; K < J; ++K) {
-      const int tJK = M + tile(J, K);
-      RC l[4][4];
+      for (int s = 0; s <= r; ++s)
+        a[r][s] -= (l[r][0] * l[s][0] + l[r][1] * l[s][1]) + (l[r][2] * l[s][2] + l[r][3] * l[s][3]);
+  }
+  int st = 0;
+  RC inv[4];
 #pragma unroll
-      for (int e = 0; e < 16; ++e) l[e >> 2][e & 3] = (c.template x<RC>(tJK + e));
+  for (int r = 0; r < 4; ++r) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
+    for (int s = 0; s <= r; ++s) {
+      RC x = a[r][s];
 #pragma unroll
-        for (int s = 0; s <= r; ++s)
-          a[r][s] -= (l[r][0] * l[s][0] + l[r][1] * l[s][1]) + (l[r][2] * l[s][2] + l[r][3] * l[s][3]);
-    }
-    RC inv[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-#pragma unroll
-      for (int s = 0; s <= r; ++s) {
-        RC x = a[r][s];
-#pragma unroll
-        for (int m = 0; m < s; ++m) x -= a[r][m] * a[s][m];
-        if (r == s) {
-          if (!(x > RC(0))) {
-            st |= 2;  // GPB_ST_CHOL_FAIL
-            x = RC(1);
-          }
-          a[r][r] = sqrt(x);
-          inv[r] = RC(1) / a[r][r];
-        } else {
-          a[r][s] = x * inv[s];
+      for (int m = 0; m < s; ++m) x -= a[r][m] * a[s][m];
+      if (r == s) {
+        if (!(x > RC(0))) {
+          st |= 2;  // GPB_ST_CHOL_FAIL
+          x = RC(1);
         }
+        a[r][r] = sqrt(x);
+        inv[r] = RC(1) / a[r][r];
+      } else {
+        a[r][s] = x * inv[s];
       }
     }
+  }
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+  for (int r = 0; r < 4; ++r) {
 #pragma unroll
-      for (int s = 0; s <= r; ++s) c.template x<RC>(tJJ + 4 * r + s) = a[r][s];
-      c.template x<RC>(c.L.D + 4 * J + r) = inv[r];
+    for (int s = 0; s <= r; ++s) c.template x<RC>(tJJ + 4 * r + s) = a[r][s];
+    c.template x<RC>(c.L.D + 4 * J + r) = inv[r];
+  }
+  return st;
+}
+
+// Off-diagonal tile (I, J), I > J: b = (A_IJ − Σ_K L_IK L_JKᵀ) L_JJ⁻ᵀ (2 FMAs
+// per loaded word).
+template <typename R, typename RC>
+__device__ __noinline__ void chol_offdiag(const LaneCtx<R>& cin, int I, int J) {
+  const LaneCtx<R> c = cin;
+  const int M = c.L.M;
+  const int tIJ = M + tile(I, J), tJJ = M + tile(J, J);
+  RC b[4][4];
+#pragma unroll
+  for (int e = 0; e < 16; ++e) b[e >> 2][e & 3] = (c.template x<RC>(tIJ + e));
+  for (int K = 0; K < J; ++K) {
+    const int tIK = M + tile(I, K), tJK = M + tile(J, K);
+    RC x[4][4], y[4][4];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      x[e >> 2][e & 3] = (c.template x<RC>(tIK + e));
+      y[e >> 2][e & 3] = (c.template x<RC>(tJK + e));
     }
-    for (int I = J + 1; I < nT; ++I) {
-      const int tIJ = M + tile(I, J);
-      RC b[4][4];
 #pragma unroll
-      for (int e = 0; e < 16; ++e) b[e >> 2][e & 3] = (c.template x<RC>(tIJ + e));
-      for (int K = 0; K < J; ++K) {
-        const int tIK = M + tile(I, K), tJK = M + tile(J, K);
-        RC x[4][4], y[4][4];
+    for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          x[e >> 2][e & 3] = (c.template x<RC>(tIK + e));
-          y[e >> 2][e & 3] = (c.template x<RC>(tJK + e));
-        }
+      for (int s = 0; s < 4; ++s)
+        b[r][s] -= (x[r][0] * y[s][0] + x[r][1] * y[s][1]) + (x[r][2] * y[s][2] + x[r][3] * y[s][3]);
+  }
+  RC a[4][4], inv[4];
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
+  for (int r = 0; r < 4; ++r) {
 #pragma unroll
-          for (int s = 0; s < 4; ++s)
-            b[r][s] -= (x[r][0] * y[s][0] + x[r][1] * y[s][1]) + (x[r][2] * y[s][2] + x[r][3] * y[s][3]);
-      }
-      // b ← b L_JJ⁻ᵀ
+    for (int s = 0; s <= r; ++s) a[r][s] = c.template x<RC>(tJJ + 4 * r + s);
+    inv[r] = c.template x<RC>(c.L.D + 4 * J + r);
+  }
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
+  for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          RC x = b[r][s];
+    for (int s = 0; s < 4; ++s) {
+      RC x = b[r][s];
 #pragma unroll
-          for (int m = 0; m < s; ++m) x -= b[r][m] * a[s][m];
-          b[r][s] = x * inv[s];
-        }
-#pragma unroll
-      for (int e = 0; e < 16; ++e) c.template x<RC>(tIJ + e) = b[e >> 2][e & 3];
+      for (int m = 0; m < s; ++m) x -= b[r][m] * a[s][m];
+      b[r][s] = x * inv[s];
     }
+#pragma unroll
+  for (int e = 0; e < 16; ++e) c.template x<RC>(tIJ + e) = b[e >> 2][e & 3];
+}
+
+// Identity padding of rows nv..4 nT−1 with I mod nw == w (n padded to a
+// multiple of 4).
+template <typename R, typename RC>
+__device__ __forceinline__ void chol_pad(const LaneCtx<R>& c, int w, int nw) {
+  const int nv = c.nv, np = ((nv + 3) >> 2) << 2;
+  for (int i = nv; i < np; ++i) {
+    if ((i >> 2) % nw != w) continue;
+    for (int j = 0; j < i; ++j) c.template x<RC>(c.L.M + tix(i, j)) = RC(0);
+    c.template x<RC>(c.L.M + tix(i, i)) = RC(1);
+    c.template x<RC>(c.L.rhs + i) = RC(0);
+  }
+}
+
+// Cholesky H = L Lᵀ (left-looking over 4×4 tiles) and the solves L y = rhs,
+// Lᵀ x = y.  Writes q̈ into `qdd`; returns GPB status bits.
+template <typename R, typename RC>
+__device__ __noinline__ int lane_cholesky_solve(const LaneCtx<R>& cin, Col<double> qdd) {
+  const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
+  const int nv = c.nv, nT = (nv + 3) >> 2;
+  chol_pad<R, RC>(c, 0, 1);
+  int st = 0;
+  for (int J = 0; J < nT; ++J) {
+    st |= chol_diag<R, RC>(cin, J);
+    for (int I = J + 1; I < nT; ++I) chol_offdiag<R, RC>(cin, I, J);
   }
   lane_solve<R, RC>(cin);
   for (int i = 0; i < nv; ++i) {
@@ -363,11 +397,14 @@ __device__ __noinline__ void lane_solve(const LaneCtx<R>& cin) {
   }
 }
 
-// One dynamics evaluation (src/dynamics.rs:322-364): reads q, v, tau (double
-// columns), writes q̈ into `qdd`.  Returns GPB status bits.
+// The sweeps of one dynamics evaluation (src/dynamics.rs:322-364): forward
+// kinematics, twists, bias accelerations, contacts and Newton–Euler outward;
+// composite inertias and joint forces inward.  Leaves each body's composite
+// inertia in the I region, the motion subspaces in S and τ + τ_spring − c in
+// rhs (in the factor's precision RC).
 template <typename R, typename RC>
-__device__ __noinline__ int lane_dynamics(const LaneCtx<R>& cin, Col<double> q, Col<double> v, Col<double> tau,
-                             bool have_tau, Col<double> qdd, Col<double> cforce, bool want_cf) {
+__device__ __noinline__ void lane_sweeps(const LaneCtx<R>& cin, Col<double> q, Col<double> v, Col<double> tau,
+                                         bool have_tau, Col<double> cforce, bool want_cf) {
   const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
   const R g = R(GRAVITY);
   // ---- outward sweep --------------------------------------------------
@@ -545,15 +582,7 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& cin, Col<double> q, 
     Ap = Ab;
   }
 
-  // ---- inward sweep: composite inertia, joint forces, CRBA fill -------
-  const int nv = c.nv;
-  if (!c.chain) {
-    // Non-ancestor pairs are not written by the fill but hold Cholesky fill-in
-    // from the previous evaluation: clear the tiled triangle first.
-    const int nT = (nv + 3) >> 2;
-    const int nm = (nT * (nT + 1) >> 1) * 16;
-    for (int e = 0; e < nm; ++e) c.template x<RC>(c.L.M + e) = RC(0);
-  }
+  // ---- inward sweep: composite inertia, joint forces ------------------
   SI<R> cI;
   SV<R> cF;
   int ctarget = -1;
@@ -566,6 +595,7 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& cin, Col<double> q, 
       iadd(Ic, cI);
       f = f + cF;
     }
+    store_si(c, c.L.I + 10 * b, Ic);
     int nvb = type == 3 ? 6 : (type == 0 ? 0 : 1);
     for (int k = 0; k < nvb; ++k) {
       SV<R> Sk = load_sv(c, c.L.S + 6 * (vo + k));
@@ -577,24 +607,6 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& cin, Col<double> q, 
       }
       // right-hand side kept in the factorisation's precision
       c.template x<RC>(c.L.rhs + vo + k) = RC(RC(rhs) - RC(sdot(Sk, f)));
-      SV<R> Fk = imul(Ic, Sk);
-      // row vo+k of H: F_kᵀ S_l for every column l of this joint and its ancestors
-      const int row = vo + k;
-      for (int l = 0; l <= k; ++l) {
-        SV<R> Sl = l == k ? Sk : load_sv(c, c.L.S + 6 * (vo + l));
-        c.template x<RC>(c.L.M + tix(row,vo + l)) = RC(sdot2(Fk, Sl));
-      }
-      int a = parent;
-      while (a != 0) {
-        uint32_t wa = c.w(2 * (a - 1));
-        int ta = wa & 15, voa = (wa >> 22) & 1023;
-        int nva = ta == 3 ? 6 : (ta == 0 ? 0 : 1);
-        for (int l = 0; l < nva; ++l) {
-          SV<R> Sl = load_sv(c, c.L.S + 6 * (voa + l));
-          c.template x<RC>(c.L.M + tix(row,voa + l)) = RC(sdot2(Fk, Sl));
-        }
-        a = (wa >> 4) & 255;
-      }
     }
     if (parent != 0) {
       int pb = parent - 1;
@@ -614,8 +626,60 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& cin, Col<double> q, 
       ctarget = -1;
     }
   }
+}
 
-  return lane_cholesky_solve<R, RC>(cin, qdd);
+// CRBA fill of the rows of H in the tile rows I with I mod nw == w (all rows
+// for nw = 1): row vo+k of body b is F_kᵀ S_l, F_k = Ic_b S_k, for every
+// column l of the joint and its ancestors (src/mechanism.rs:592-696).  For a
+// tree that is not a chain the owned tile rows are cleared first (non-ancestor
+// pairs hold fill-in of the previous factor).  One compiled function serves
+// the one-warp and the block-cooperative paths, so both round identically.
+template <typename R, typename RC>
+__device__ __noinline__ void lane_fill(const LaneCtx<R>& cin, int w, int nw) {
+  const LaneCtx<R> c = cin;
+  const int nT = (c.nv + 3) >> 2;
+  if (!c.chain) {
+    for (int I = w; I < nT; I += nw)
+      for (int e = tile(I, 0); e < tile(I, I) + 16; ++e) c.template x<RC>(c.L.M + e) = RC(0);
+  }
+  for (int b = 0; b < c.nb; ++b) {
+    const uint32_t w0 = c.w(2 * b);
+    const int type = w0 & 15, parent = (w0 >> 4) & 255, vo = (w0 >> 22) & 1023;
+    const int nvb = type == 3 ? 6 : (type == 0 ? 0 : 1);
+    if (nvb == 0) continue;
+    const SI<R> Ic = load_si(c, c.L.I + 10 * b);
+    for (int k = 0; k < nvb; ++k) {
+      const int row = vo + k;
+      if ((row >> 2) % nw != w) continue;
+      const SV<R> Sk = load_sv(c, c.L.S + 6 * row);
+      const SV<R> Fk = imul(Ic, Sk);
+      for (int l = 0; l <= k; ++l) {
+        const SV<R> Sl = l == k ? Sk : load_sv(c, c.L.S + 6 * (vo + l));
+        c.template x<RC>(c.L.M + tix(row, vo + l)) = RC(sdot2(Fk, Sl));
+      }
+      int a = parent;
+      while (a != 0) {
+        const uint32_t wa = c.w(2 * (a - 1));
+        const int ta = wa & 15, voa = (wa >> 22) & 1023;
+        const int nva = ta == 3 ? 6 : (ta == 0 ? 0 : 1);
+        for (int l = 0; l < nva; ++l) {
+          const SV<R> Sl = load_sv(c, c.L.S + 6 * (voa + l));
+          c.template x<RC>(c.L.M + tix(row, voa + l)) = RC(sdot2(Fk, Sl));
+        }
+        a = (wa >> 4) & 255;
+      }
+    }
+  }
+}
+
+// One dynamics evaluation (src/dynamics.rs:322-364): reads q, v, tau (double
+// columns), writes q̈ into `qdd`.  Returns GPB status bits.
+template <typename R, typename RC>
+__device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<double> tau,
+                                          bool have_tau, Col<double> qdd, Col<double> cforce, bool want_cf) {
+  lane_sweeps<R, RC>(c, q, v, tau, have_tau, cforce, want_cf);
+  lane_fill<R, RC>(c, 0, 1);
+  return lane_cholesky_solve<R, RC>(c, qdd);
 }
 
 #include "gpb_link.cuh"
@@ -863,14 +927,30 @@ struct EvalOf<2> {
   }
 };
 
+#include "gpb_coop.cuh"
+
 template <int PREC>
 __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams p) {
   const int lane = threadIdx.x & 31;
+  // packs [0, ncoop): one whole block per pack (large mechanisms, largest first)
+  if (PREC != 2 && p.ncoop > 0) {
+    __shared__ CoopShared sh;
+    __shared__ int s_pk;
+    while (true) {
+      if (threadIdx.x == 0) s_pk = atomicAdd(b.queue + 1, 1);
+      __syncthreads();
+      const int pk = s_pk;
+      __syncthreads();
+      if (pk >= p.ncoop) break;
+      coop_pack<PREC == 2 ? 0 : PREC>(b, p, pk, &sh);
+    }
+  }
+  // the rest: one warp per pack
   const int32_t nwork = b.active ? b.nactive : b.npacks;
   while (true) {
     int pk = 0;
     if (lane == 0) {
-      const int w = atomicAdd(b.queue, 1);
+      const int w = atomicAdd(b.queue, 1) + (b.active ? 0 : p.ncoop);
       pk = w >= nwork ? -1 : (b.active ? b.active[w] : w);
     }
     pk = __shfl_sync(0xffffffffu, pk, 0);
@@ -1015,7 +1095,7 @@ cudaError_t launch_gather_words(const void* src, int bytes, const int64_t* idx, 
 cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes_per_instance,
                             int num_sms, int warps_per_sm, cudaStream_t s) {
   (void)lanes_per_instance;
-  cudaError_t e = cudaMemsetAsync(b.queue, 0, sizeof(int32_t), s);
+  cudaError_t e = cudaMemsetAsync(b.queue, 0, 2 * sizeof(int32_t), s);
   if (e != cudaSuccess) return e;
   const int threads = 128;
   int per_sm = 0;

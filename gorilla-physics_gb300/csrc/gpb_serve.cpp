@@ -288,7 +288,7 @@ extern "C" int gpb_server_create(gpb_ctx* ctx, const gpb_server_opts* o, gpb_ser
   chk(B.v.alloc(rv * L));
   chk(B.tau_in.alloc(rv * L));
   chk(B.scratch.alloc(rs * L));
-  chk(B.queue.alloc(1));
+  chk(B.queue.alloc(2));
   chk(S->jobs.alloc(npacks * L));
   chk(S->active.alloc(std::max<int32_t>(npacks, 1)));
   chk(S->finished.alloc(std::max<size_t>(npacks * L, 1)));

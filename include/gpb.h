@@ -270,6 +270,25 @@ int gpb_batch_set_mapping(gpb_batch* batch, int lanes_per_instance);
  * SM's four schedulers (each with its own FP64 unit) runs one pack at a time. */
 int gpb_batch_set_launch(gpb_batch* batch, int warps_per_sm);
 
+/* Packs whose every instance has at least `min_dof` DOF are stepped by a whole
+ * 4-warp block (one warp per scheduler): warp 0 runs the sweeps, the four
+ * warps share the mass-matrix fill and the Cholesky factorisation.  Results
+ * are bit-identical to the one-warp path; large mechanisms finish sooner, which
+ * shortens the critical path of a batch with a wide size range.  -1 = the
+ * library's default, 0 = off.  Not used by GPB_MIXED_REFINED. */
+int gpb_batch_set_coop(gpb_batch* batch, int min_dof);
+
+/* Autotuner: times `trial_steps` steps of this batch (its own mechanisms,
+ * state, step size, integrator, precision and control law) for each launch
+ * shape (4 or 8 resident warps per SM; block-cooperative packs off or from 32 /
+ * 40 DOF when the batch has such packs), keeps the fastest with
+ * gpb_batch_set_launch / gpb_batch_set_coop and reports it.  The batch's q, v,
+ * torques and status words are restored afterwards; results of later calls do
+ * not depend on the choice (every shape computes the same bits). */
+int gpb_batch_autotune(gpb_batch* batch, double dt, int integrator, int precision,
+                       const gpb_control_params* control, int trial_steps, int* warps_per_sm,
+                       int* coop_min_dof);
+
 /* Number of this library's kernel launches issued by the context so far. */
 int64_t gpb_launch_count(const gpb_ctx* ctx);
 
