@@ -1,0 +1,729 @@
+// Articulated-body algorithm (included by gpb_kernels.cu after gpb_link.cuh).
+//
+// Featherstone, "Rigid Body Dynamics Algorithms", Table 7.1: q̈ in three O(n)
+// passes over the tree in link coordinates — velocities and bias terms
+// outward, articulated inertias and bias forces inward, accelerations
+// outward — instead of the reference's CRBA mass matrix and dense solve
+// (src/dynamics.rs:255-276, src/mechanism.rs:592-696).  The same q̈ in exact
+// arithmetic; no O(n²) fill and no O(n³) factorisation, so a 48-DOF chain
+// costs about half the FP64 work and its critical path shrinks accordingly.
+//
+// Precision: kinematics, bias forces and the final accelerations run in R
+// (double for GPB_FP64, float for GPB_MIXED).  The articulated inertias, the
+// projections U = I^A S, D = Sᵀ U and the congruence X*ᵀ I^a X to the parent
+// frame always run in FP64: that recursion subtracts U D⁻¹ Uᵀ from I^A and is
+// where FP32 loses digits on long chains (FP32 everywhere gives q̈ errors up to
+// 2e-5 of |q̈| on 48-DOF chains; FP64 here keeps them below 1e-5).  The poses
+// that place contact points are computed in FP64 whenever an instance has
+// contacts (a penetration error ε·|p| becomes a force error k·ε·|p|).
+#pragma once
+
+// Symmetric 6×6 spatial inertia in blocks [[A, B], [Bᵀ, C]] acting on (ω, v):
+// A, C symmetric (xx, yy, zz, xy, xz, yz), B row-major.  A rigid body's is
+// A = J, B = [c]×, C = m·1 (the convention of imul).
+struct ABI {
+  double A[6], B[9], C[6];
+};
+constexpr int ABI_D = 21;
+
+__device__ __forceinline__ double symget(const double* S, int i, int j) {
+  // (0,0)=0 (1,1)=1 (2,2)=2 (0,1)=3 (0,2)=4 (1,2)=5
+  if (i == j) return S[i];
+  const int a = i < j ? i : j, b = i < j ? j : i;
+  return S[a == 0 ? (b == 1 ? 3 : 4) : 5];
+}
+
+template <typename R>
+__device__ __forceinline__ void store_abi(const LaneCtx<R>& c, int base, const ABI& I) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) c.d(base + k) = I.A[k];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) c.d(base + 6 + k) = I.B[k];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) c.d(base + 15 + k) = I.C[k];
+}
+template <typename R>
+__device__ __forceinline__ ABI load_abi(const LaneCtx<R>& c, int base) {
+  ABI I;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) I.A[k] = c.d(base + k);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) I.B[k] = c.d(base + 6 + k);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) I.C[k] = c.d(base + 15 + k);
+  return I;
+}
+__device__ __forceinline__ void abi_add(ABI& a, const ABI& b) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) a.A[k] += b.A[k];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) a.B[k] += b.B[k];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) a.C[k] += b.C[k];
+}
+
+// Rigid-body inertia from the topology table (mass, m·com, J about the origin).
+template <typename R>
+__device__ __forceinline__ ABI body_abi(const LaneCtx<R>& c, int tb) {
+  ABI I;
+  const double m = c.td(tb + TD_INERTIA);
+  const double cx = c.td(tb + TD_INERTIA + 1), cy = c.td(tb + TD_INERTIA + 2), cz = c.td(tb + TD_INERTIA + 3);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) I.A[k] = c.td(tb + TD_INERTIA + 4 + k);
+  I.B[0] = 0.0, I.B[1] = -cz, I.B[2] = cy;
+  I.B[3] = cz, I.B[4] = 0.0, I.B[5] = -cx;
+  I.B[6] = -cy, I.B[7] = cx, I.B[8] = 0.0;
+  I.C[0] = I.C[1] = I.C[2] = m;
+  I.C[3] = I.C[4] = I.C[5] = 0.0;
+  return I;
+}
+
+// I·(w, v) = (A w + B v, Bᵀ w + C v).
+__device__ __forceinline__ void abi_mul(const ABI& I, const double* w, const double* v, double* ow, double* ov) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    ow[i] = symget(I.A, i, 0) * w[0] + symget(I.A, i, 1) * w[1] + symget(I.A, i, 2) * w[2] +
+            I.B[3 * i] * v[0] + I.B[3 * i + 1] * v[1] + I.B[3 * i + 2] * v[2];
+    ov[i] = I.B[i] * w[0] + I.B[3 + i] * w[1] + I.B[6 + i] * w[2] + symget(I.C, i, 0) * v[0] +
+            symget(I.C, i, 1) * v[1] + symget(I.C, i, 2) * v[2];
+  }
+}
+
+// S' = R S Rᵀ for symmetric S.
+__device__ __forceinline__ void sym_rotate(const double* R, const double* S, double* out) {
+  double P[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      P[3 * i + j] = R[3 * i] * symget(S, 0, j) + R[3 * i + 1] * symget(S, 1, j) + R[3 * i + 2] * symget(S, 2, j);
+  const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+    out[k] = P[3 * ii[k]] * R[3 * jj[k]] + P[3 * ii[k] + 1] * R[3 * jj[k] + 1] + P[3 * ii[k] + 2] * R[3 * jj[k] + 2];
+}
+// B' = R B Rᵀ for general B.
+__device__ __forceinline__ void gen_rotate(const double* R, const double* B, double* out) {
+  double P[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) P[3 * i + j] = R[3 * i] * B[j] + R[3 * i + 1] * B[3 + j] + R[3 * i + 2] * B[6 + j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      out[3 * i + j] = P[3 * i] * R[3 * j] + P[3 * i + 1] * R[3 * j + 1] + P[3 * i + 2] * R[3 * j + 2];
+}
+
+// Rotation about principal axis k by (cos, sin), applied to the rows of a
+// 3-column block (x_i1' = c x_i1 − s x_i2, x_i2' = s x_i1 + c x_i2 with
+// i1 = k+1, i2 = k+2 mod 3) or to its columns.
+__device__ __forceinline__ void planar_rows(double* M, int k, double co, double si) {
+  const int i1 = (k + 1) % 3, i2 = (k + 2) % 3;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double a = M[3 * i1 + j], b = M[3 * i2 + j];
+    M[3 * i1 + j] = co * a - si * b;
+    M[3 * i2 + j] = si * a + co * b;
+  }
+}
+__device__ __forceinline__ void planar_cols(double* M, int k, double co, double si) {
+  const int i1 = (k + 1) % 3, i2 = (k + 2) % 3;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const double a = M[3 * r + i1], b = M[3 * r + i2];
+    M[3 * r + i1] = co * a - si * b;
+    M[3 * r + i2] = si * a + co * b;
+  }
+}
+// R S Rᵀ for symmetric S (packed) and the rotation about principal axis k:
+// only the (i1, i2) plane mixes.
+__device__ __forceinline__ void sym_planar(double* S, int k, double co, double si) {
+  const int i1 = (k + 1) % 3, i2 = (k + 2) % 3;
+  // packed index of (i, j)
+  auto pk = [](int i, int j) { return i == j ? i : ((i + j == 1) ? 3 : ((i + j == 2) ? 4 : 5)); };
+  const double a = S[pk(i1, i1)], b = S[pk(i2, i2)], d = S[pk(i1, i2)];
+  const double e1 = S[pk(i1, k)], e2 = S[pk(i2, k)];
+  const double c2 = co * co, s2 = si * si, cs = co * si;
+  const double cs2d = 2.0 * cs * d;
+  S[pk(i1, i1)] = c2 * a + s2 * b - cs2d;
+  S[pk(i2, i2)] = s2 * a + c2 * b + cs2d;
+  S[pk(i1, i2)] = cs * (a - b) + (c2 - s2) * d;
+  S[pk(i1, k)] = co * e1 - si * e2;
+  S[pk(i2, k)] = si * e1 + co * e2;
+}
+
+__device__ __forceinline__ void sym_expand(const double* S, double* F) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) F[3 * i + j] = symget(S, i, j);
+}
+__device__ __forceinline__ void sym_pack(const double* F, double* S) {
+  S[0] = F[0], S[1] = F[4], S[2] = F[8], S[3] = F[1], S[4] = F[2], S[5] = F[5];
+}
+
+// Articulated inertia of a child, in the child frame, expressed in the parent
+// frame: X*ᵀ I X for the child→parent transform (rotation Rr, child origin t).
+// Rotation of every block, then the shift by t (T = [t]×):
+//   C_p = C', B_p = B' + T C', A_p = A' − B'T − (B'T)ᵀ − T C' T.
+// `planar` ≥ 0: Rr is the rotation about principal axis `planar` by (co, si).
+__device__ __forceinline__ ABI abi_to_parent(const ABI& I, const double* Rr, V3<double> t, int planar, double co,
+                                             double si) {
+  double A[9], B[9], Cm[9];
+  if (planar >= 0) {
+    double a6[6], c6[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      a6[k] = I.A[k];
+      c6[k] = I.C[k];
+    }
+    sym_planar(a6, planar, co, si);
+    sym_planar(c6, planar, co, si);
+    sym_expand(a6, A);
+    sym_expand(c6, Cm);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) B[k] = I.B[k];
+    planar_rows(B, planar, co, si);
+    planar_cols(B, planar, co, si);
+  } else {
+    double a6[6], c6[6];
+    sym_rotate(Rr, I.A, a6);
+    sym_rotate(Rr, I.C, c6);
+    gen_rotate(Rr, I.B, B);
+    sym_expand(a6, A);
+    sym_expand(c6, Cm);
+  }
+  // T = [t]×: rows (0, −tz, ty), (tz, 0, −tx), (−ty, tx, 0)
+  double W[9], BT[9];  // W = T C', BT = B' T
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    W[j] = -t.z * Cm[3 + j] + t.y * Cm[6 + j];
+    W[3 + j] = t.z * Cm[j] - t.x * Cm[6 + j];
+    W[6 + j] = -t.y * Cm[j] + t.x * Cm[3 + j];
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    BT[3 * i] = B[3 * i + 1] * t.z - B[3 * i + 2] * t.y;
+    BT[3 * i + 1] = -B[3 * i] * t.z + B[3 * i + 2] * t.x;
+    BT[3 * i + 2] = B[3 * i] * t.y - B[3 * i + 1] * t.x;
+  }
+  ABI o;
+  const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const int i = ii[k], j = jj[k];
+    // (T C' T)_ij = (W T)_ij
+    const double wt = j == 0 ? (W[3 * i + 1] * t.z - W[3 * i + 2] * t.y)
+                             : (j == 1 ? (-W[3 * i] * t.z + W[3 * i + 2] * t.x) : (W[3 * i] * t.y - W[3 * i + 1] * t.x));
+    o.A[k] = A[3 * i + j] - BT[3 * i + j] - BT[3 * j + i] - wt;
+    o.C[k] = Cm[3 * i + j];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) o.B[k] = B[k] + W[k];
+  return o;
+}
+
+// 6×6 Cholesky of a spatial inertia (packed lower triangle L[21], reciprocal
+// diagonal) and the solve L Lᵀ x = b.  Returns false for a non-positive pivot.
+__device__ __forceinline__ int l6(int i, int j) { return (i * (i + 1) >> 1) + j; }
+__device__ __forceinline__ bool chol6(const ABI& I, double* L, double* dinv) {
+  double M6[21];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      double x;
+      if (i < 3) x = symget(I.A, i, j);
+      else if (j < 3) x = I.B[3 * j + (i - 3)];  // block (v, ω) = Bᵀ
+      else x = symget(I.C, i - 3, j - 3);
+      M6[l6(i, j)] = x;
+    }
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      double x = M6[l6(i, j)];
+#pragma unroll
+      for (int k = 0; k < j; ++k) x -= L[l6(i, k)] * L[l6(j, k)];
+      if (i == j) {
+        if (!(x > 0.0)) {
+          ok = false;
+          x = 1.0;
+        }
+        L[l6(i, i)] = sqrt(x);
+        dinv[i] = 1.0 / L[l6(i, i)];
+      } else {
+        L[l6(i, j)] = x * dinv[j];
+      }
+    }
+  }
+  return ok;
+}
+__device__ __forceinline__ void solve6(const double* L, const double* dinv, double* x) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double s = x[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) s -= L[l6(i, k)] * x[k];
+    x[i] = s * dinv[i];
+  }
+#pragma unroll
+  for (int i = 5; i >= 0; --i) {
+    double s = x[i];
+#pragma unroll
+    for (int k = i + 1; k < 6; ++k) s -= L[l6(k, i)] * x[k];
+    x[i] = s * dinv[i];
+  }
+}
+
+// Per-DOF record of the inward pass (DU region, 11 words per DOF):
+//   1-DOF joint: U (6), 1/D, u
+//   floating joint (its 6 DOF slots, 66 words): L (21), 1/diag (6), u (6)
+constexpr int DU_D = 11;
+
+// I·(w, v) in the sweep precision R (the bias-force update needs only R).
+template <typename R>
+__device__ __forceinline__ SV<R> abi_mul_r(const ABI& I, const SV<R>& x) {
+  R A[6], B[9], C[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    A[k] = R(I.A[k]);
+    C[k] = R(I.C[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) B[k] = R(I.B[k]);
+  const R w[3] = {x.w.x, x.w.y, x.w.z}, v[3] = {x.v.x, x.v.y, x.v.z};
+  R ow[3], ov[3];
+  const int s[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    ow[i] = A[s[i][0]] * w[0] + A[s[i][1]] * w[1] + A[s[i][2]] * w[2] + B[3 * i] * v[0] + B[3 * i + 1] * v[1] +
+            B[3 * i + 2] * v[2];
+    ov[i] = B[i] * w[0] + B[3 + i] * w[1] + B[6 + i] * w[2] + C[s[i][0]] * v[0] + C[s[i][1]] * v[1] +
+            C[s[i][2]] * v[2];
+  }
+  return {{ow[0], ow[1], ow[2]}, {ov[0], ov[1], ov[2]}};
+}
+
+// (Rrel, t) of body b in the sweep precision: the FP64 record in the I
+// region, or (R = float) its FP32 copy in RF.
+template <typename R>
+__device__ __forceinline__ void load_xf(const LaneCtx<R>& c, int b, M3<R>& Rr, V3<R>& t) {
+  if (sizeof(R) == 8) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Rr.a[k] = R(c.d(c.L.I + 12 * b + k));
+    t = {R(c.d(c.L.I + 12 * b + 9)), R(c.d(c.L.I + 12 * b + 10)), R(c.d(c.L.I + 12 * b + 11))};
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Rr.a[k] = c.r(c.L.RF + 12 * b + k);
+    t = {c.r(c.L.RF + 12 * b + 9), c.r(c.L.RF + 12 * b + 10), c.r(c.L.RF + 12 * b + 11)};
+  }
+}
+
+// One dynamics evaluation by the articulated-body algorithm.  q̈ into qdd;
+// GPB status bits (CHOL_FAIL for a non-positive articulated inertia D).
+template <typename R>
+__device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<double> v, Col<double> tau,
+                                     bool have_tau, Col<double> qdd, Col<double> cf, bool want_cf) {
+  const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
+  using V = V3<R>;
+  using VD = V3<double>;
+  const bool contacts = c.nc > 0;
+  const bool wide = contacts || sizeof(R) == 8;  // FP64 joint transforms
+  const V zero{R(0), R(0), R(0)};
+  V pw_ = zero, pv_ = zero;                  // parent velocity (chain carry)
+  VD ppos{0.0, 0.0, 0.0};
+  M3<double> pR = eye3<double>();            // parent world pose (contacts only)
+  int st = 0;
+  // ---- pass 1 (outward): transforms, velocities, bias terms, contacts ------
+  for (int b = 0; b < c.nb; ++b) {
+    const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
+    const int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
+    const uint32_t fl = w1 & 255;
+    V om = zero, vl = zero;
+    VD posw{0.0, 0.0, 0.0};
+    M3<double> Rw = eye3<double>();
+    if (parent == b && parent != 0) {
+      om = pw_;
+      vl = pv_;
+      posw = ppos;
+      Rw = pR;
+    } else if (parent != 0) {
+      const int pb = parent - 1;
+      om = {c.r(c.L.V + 6 * pb), c.r(c.L.V + 6 * pb + 1), c.r(c.L.V + 6 * pb + 2)};
+      vl = {c.r(c.L.V + 6 * pb + 3), c.r(c.L.V + 6 * pb + 4), c.r(c.L.V + 6 * pb + 5)};
+      if (contacts) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Rw.a[k] = c.d(c.L.X + 12 * pb + k);
+        posw = {c.d(c.L.X + 12 * pb + 9), c.d(c.L.X + 12 * pb + 10), c.d(c.L.X + 12 * pb + 11)};
+      }
+    }
+    // child → parent transform (Rr, t): FP64 record Rd / td; Rr, t in R
+    const int tb = TOPO_D * b;
+    const bool rid = (fl & BF_INIT_ROT_IDENTITY) != 0;
+    const bool planar = type == 1 && rid && (fl & BF_AXIS_PRINCIPAL);
+    M3<double> Rd = eye3<double>();
+    VD td{c.td(tb + TD_TINIT), c.td(tb + TD_TINIT + 1), c.td(tb + TD_TINIT + 2)};
+    M3<R> Rr;
+    if (planar) {  // rotation about ±e_k: only the (k+1, k+2) plane turns
+      const int k = (int)bf_axis_index(fl), i1 = (k + 1) % 3, i2 = (k + 2) % 3;
+      double co, si;
+      R cor, sir;
+      if (wide) {
+        sincos(q[qo], &si, &co);
+        cor = R(co);
+        sir = R(si);
+      } else {
+        float sf, cfl;
+        sincos_q<float>(q[qo], &sf, &cfl);
+        cor = R(cfl);
+        sir = R(sf);
+        co = cfl;
+        si = sf;
+      }
+      if (fl & BF_AXIS_NEG) {
+        si = -si;
+        sir = -sir;
+      }
+      Rd.a[3 * i1 + i1] = co;
+      Rd.a[3 * i1 + i2] = -si;
+      Rd.a[3 * i2 + i1] = si;
+      Rd.a[3 * i2 + i2] = co;
+#pragma unroll
+      for (int e = 0; e < 9; ++e) Rr.a[e] = (e % 4 == 0) ? R(1) : R(0);
+      Rr.a[3 * i1 + i1] = cor;
+      Rr.a[3 * i1 + i2] = -sir;
+      Rr.a[3 * i2 + i1] = sir;
+      Rr.a[3 * i2 + i2] = cor;
+    } else {
+      M3<double> Rid = eye3<double>();
+      if (!rid) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Rid.a[k] = c.td(tb + TD_RINIT + k);
+      }
+      VD axd{0.0, 0.0, 0.0};
+      if (type == 1 || type == 2) axd = {c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
+      if (type == 1) {
+        double co, si;
+        if (wide) {
+          sincos(q[qo], &si, &co);
+        } else {
+          float sf, cfl;
+          sincos_q<float>(q[qo], &sf, &cfl);
+          si = sf;
+          co = cfl;
+        }
+        const double omc = 1.0 - co;  // Rot(a, q) = c 1 + s [a]× + (1 − c) a aᵀ
+        M3<double> Ro;
+        Ro.a[0] = co + axd.x * axd.x * omc;
+        Ro.a[1] = axd.x * axd.y * omc - axd.z * si;
+        Ro.a[2] = axd.x * axd.z * omc + axd.y * si;
+        Ro.a[3] = axd.y * axd.x * omc + axd.z * si;
+        Ro.a[4] = co + axd.y * axd.y * omc;
+        Ro.a[5] = axd.y * axd.z * omc - axd.x * si;
+        Ro.a[6] = axd.z * axd.x * omc - axd.y * si;
+        Ro.a[7] = axd.z * axd.y * omc + axd.x * si;
+        Ro.a[8] = co + axd.z * axd.z * omc;
+        Rd = rid ? Ro : mul(Rid, Ro);
+      } else if (type == 2) {
+        Rd = Rid;
+        td = td + mul(Rid, axd * q[qo]);
+      } else if (type == 3) {
+        const M3<double> Rq = quat_to_mat<double>(q[qo], q[qo + 1], q[qo + 2], q[qo + 3]);
+        const VD tq{q[qo + 4], q[qo + 5], q[qo + 6]};
+        Rd = rid ? Rq : mul(Rid, Rq);
+        td = td + mul(Rid, tq);
+      } else {
+        Rd = Rid;
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Rr.a[k] = R(Rd.a[k]);
+    }
+    const V t{R(td.x), R(td.y), R(td.z)};
+    // velocity: v = X v_p + S q̇ ; bias acceleration c = v ×m (S q̇)
+    vl = mulT(Rr, vl + cross(om, t));
+    om = mulT(Rr, om);
+    V jw = zero, jv = zero;
+    if (type == 1 || type == 2) {
+      const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
+      if (type == 1) jw = ax * R(v[vo]);
+      else jv = ax * R(v[vo]);
+    } else if (type == 3) {
+      jw = {R(v[vo]), R(v[vo + 1]), R(v[vo + 2])};
+      jv = {R(v[vo + 3]), R(v[vo + 4]), R(v[vo + 5])};
+    }
+    om = om + jw;
+    vl = vl + jv;
+    const SV<R> cb{cross(om, jw), cross(om, jv) + cross(vl, jw)};
+    // bias force p = v ×* I v − f_contact (body frame)
+    SI<R> I;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) I.j[k] = c.t(tb + TD_INERTIA + 4 + k);
+    I.c = {c.t(tb + TD_INERTIA + 1), c.t(tb + TD_INERTIA + 2), c.t(tb + TD_INERTIA + 3)};
+    I.m = c.t(tb + TD_INERTIA);
+    const SV<R> vb{om, vl};
+    SV<R> p = crf(vb, imul(I, vb));
+    if (contacts) {
+      posw = posw + mul(Rw, td);
+      Rw = mul(Rw, Rd);
+      const int cb0 = (w1 >> 8) & 255, cn = (w1 >> 16) & 255;
+      if (cn) {
+        const VD omd{double(om.x), double(om.y), double(om.z)}, vld{double(vl.x), double(vl.y), double(vl.z)};
+        const VD omw = mul(Rw, omd), vw = mul(Rw, vld);
+        for (int k = cb0; k < cb0 + cn; ++k) {
+          const int cd = CTC_D * k;
+          const VD loc{c.cdd(cd), c.cdd(cd + 1), c.cdd(cd + 2)};
+          const double kp = c.cdd(cd + 3), rad = c.cdd(cd + 4), damp = c.cdd(cd + 5);
+          const VD pwc = mul(Rw, loc) + posw;
+          VD fsum{0.0, 0.0, 0.0};
+          for (int h = 0; h < c.nh; ++h) {
+            const int hd = HS_D * h;
+            const VD hp{c.hdd(hd), c.hdd(hd + 1), c.hdd(hd + 2)};
+            const VD hn{c.hdd(hd + 3), c.hdd(hd + 4), c.hdd(hd + 5)};
+            const double alh = c.hdd(hd + 6), mu = c.hdd(hd + 7);
+            const double dist = dot(pwc - hp, hn);
+            VD app = pwc;
+            double pen;
+            if (rad > 0.0) {
+              if (!(dist - rad <= 1e-8)) continue;
+              pen = rad - dist;
+              app = pwc - hn * rad;
+            } else {
+              if (!(dist <= 1e-8)) continue;  // HalfSpace::has_inside (margin 1e-8)
+              pen = -dist;
+            }
+            const VD vel = vw + cross(omw, app - posw);
+            const VD fc = contact_force<double>(c.model, pen, hn, vel, kp, damp, alh, mu);
+            const VD fbd = mulT(Rw, fc), rbd = mulT(Rw, app - posw);
+            const VD nb = cross(rbd, fbd);
+            p.w = p.w - V{R(nb.x), R(nb.y), R(nb.z)};
+            p.v = p.v - V{R(fbd.x), R(fbd.y), R(fbd.z)};
+            fsum = fsum + fc;
+          }
+          if (want_cf) {
+            const int orig = (c.CI[(size_t)k * LANES] >> 8) & 255;
+            cf[3 * orig] = fsum.x;
+            cf[3 * orig + 1] = fsum.y;
+            cf[3 * orig + 2] = fsum.z;
+          }
+        }
+      }
+    }
+    // records for the inward and second outward passes
+#pragma unroll
+    for (int k = 0; k < 9; ++k) c.d(c.L.I + 12 * b + k) = Rd.a[k];
+    c.d(c.L.I + 12 * b + 9) = td.x;
+    c.d(c.L.I + 12 * b + 10) = td.y;
+    c.d(c.L.I + 12 * b + 11) = td.z;
+    if (sizeof(R) == 4) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) c.r(c.L.RF + 12 * b + k) = Rr.a[k];
+      c.r(c.L.RF + 12 * b + 9) = t.x;
+      c.r(c.L.RF + 12 * b + 10) = t.y;
+      c.r(c.L.RF + 12 * b + 11) = t.z;
+    }
+    store_sv(c, c.L.A + 6 * b, cb);
+    store_sv(c, c.L.F + 6 * b, p);
+    store_abi(c, c.L.AI + ABI_D * b, body_abi(c, tb));
+    if (fl & BF_BRANCH) {
+      store_sv(c, c.L.V + 6 * b, vb);
+      if (contacts) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) c.d(c.L.X + 12 * b + k) = Rw.a[k];
+        c.d(c.L.X + 12 * b + 9) = posw.x;
+        c.d(c.L.X + 12 * b + 10) = posw.y;
+        c.d(c.L.X + 12 * b + 11) = posw.z;
+      }
+    }
+    pw_ = om;
+    pv_ = vl;
+    ppos = posw;
+    pR = Rw;
+  }
+  // ---- pass 2 (inward): articulated inertias and bias forces --------------
+  for (int b = c.nb - 1; b >= 0; --b) {
+    const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
+    const uint32_t fl = w1 & 255;
+    const int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
+    const int tb = TOPO_D * b;
+    ABI IA = load_abi(c, c.L.AI + ABI_D * b);
+    const SV<R> pA = load_sv(c, c.L.F + 6 * b);
+    const SV<R> cb = load_sv(c, c.L.A + 6 * b);
+    SV<R> pa;  // bias force handed to the parent
+    const bool to_parent = parent != 0;
+    if (type == 1 || type == 2) {
+      double Uw[3], Uv[3], D;
+      if (type == 1 && (fl & BF_AXIS_PRINCIPAL)) {  // a = ±e_k: U = ±(A[:,k], row k of B), D = A_kk
+        const int k = (int)bf_axis_index(fl);
+        const double sg = (fl & BF_AXIS_NEG) ? -1.0 : 1.0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          Uw[i] = sg * symget(IA.A, i, k);
+          Uv[i] = sg * IA.B[3 * k + i];
+        }
+        D = IA.A[k];
+      } else {
+        const double ax[3] = {c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
+        if (type == 1) {  // U = I (a, 0) = (A a, Bᵀ a)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            Uw[i] = symget(IA.A, i, 0) * ax[0] + symget(IA.A, i, 1) * ax[1] + symget(IA.A, i, 2) * ax[2];
+            Uv[i] = IA.B[i] * ax[0] + IA.B[3 + i] * ax[1] + IA.B[6 + i] * ax[2];
+          }
+          D = ax[0] * Uw[0] + ax[1] * Uw[1] + ax[2] * Uw[2];
+        } else {  // U = I (0, a) = (B a, C a)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            Uw[i] = IA.B[3 * i] * ax[0] + IA.B[3 * i + 1] * ax[1] + IA.B[3 * i + 2] * ax[2];
+            Uv[i] = symget(IA.C, i, 0) * ax[0] + symget(IA.C, i, 1) * ax[1] + symget(IA.C, i, 2) * ax[2];
+          }
+          D = ax[0] * Uv[0] + ax[1] * Uv[1] + ax[2] * Uv[2];
+        }
+      }
+      // u = τ + τ_spring − Sᵀ p^A
+      const V axr{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
+      double u = have_tau ? tau[vo] : 0.0;
+      if (type == 2 && (w1 & BF_SPRING)) u += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
+      u -= double(type == 1 ? dot(axr, pA.w) : dot(axr, pA.v));
+      if (!(D > 0.0)) st |= 2;  // GPB_ST_CHOL_FAIL
+      const double Dinv = 1.0 / D;
+      const int du = c.L.DU + DU_D * vo;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        c.d(du + i) = Uw[i];
+        c.d(du + 3 + i) = Uv[i];
+      }
+      c.d(du + 6) = Dinv;
+      c.d(du + 7) = u;
+      if (to_parent) {
+        // I^a = I^A − U D⁻¹ Uᵀ (FP64) ; p^a = p^A + I^a c + U D⁻¹ u (R)
+        double Ww[3], Wv[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          Ww[i] = Uw[i] * Dinv;
+          Wv[i] = Uv[i] * Dinv;
+        }
+        const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          IA.A[k] -= Ww[ii[k]] * Uw[jj[k]];
+          IA.C[k] -= Wv[ii[k]] * Uv[jj[k]];
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) IA.B[3 * i + j] -= Ww[i] * Uv[j];
+        const R ud = R(u * Dinv);
+        const SV<R> Ur{{R(Uw[0]), R(Uw[1]), R(Uw[2])}, {R(Uv[0]), R(Uv[1]), R(Uv[2])}};
+        pa = pA + abi_mul_r<R>(IA, cb) + scale(Ur, ud);
+      }
+    } else if (type == 3) {
+      double L[21], dinv[6];
+      if (!chol6(IA, L, dinv)) st |= 2;
+      const int du = c.L.DU + DU_D * vo;
+#pragma unroll
+      for (int k = 0; k < 21; ++k) c.d(du + k) = L[k];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) c.d(du + 21 + k) = dinv[k];
+      const R pv6[6] = {pA.w.x, pA.w.y, pA.w.z, pA.v.x, pA.v.y, pA.v.z};
+      R pa6[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const double u = (have_tau ? tau[vo + k] : 0.0) - double(pv6[k]);
+        c.d(du + 27 + k) = u;
+        pa6[k] = R(double(pv6[k]) + u);  // floating joint: I^a = 0, p^a = p^A + u
+      }
+      pa = {{pa6[0], pa6[1], pa6[2]}, {pa6[3], pa6[4], pa6[5]}};
+    } else {  // fixed joint: I^a = I^A, p^a = p^A + I^A c
+      pa = pA + abi_mul_r<R>(IA, cb);
+    }
+    if (to_parent) {
+      const int pb = parent - 1;
+      if (type != 3) {
+        double Rr[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Rr[k] = c.d(c.L.I + 12 * b + k);
+        const VD t{c.d(c.L.I + 12 * b + 9), c.d(c.L.I + 12 * b + 10), c.d(c.L.I + 12 * b + 11)};
+        int planar = -1;
+        double co = 1.0, si = 0.0;
+        if (type == 1 && (fl & BF_INIT_ROT_IDENTITY) && (fl & BF_AXIS_PRINCIPAL)) {
+          planar = (int)bf_axis_index(fl);
+          const int i1 = (planar + 1) % 3, i2 = (planar + 2) % 3;
+          co = Rr[3 * i1 + i1];
+          si = Rr[3 * i2 + i1];
+        }
+        ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si);
+        ABI acc = load_abi(c, c.L.AI + ABI_D * pb);
+        abi_add(acc, Ip);
+        store_abi(c, c.L.AI + ABI_D * pb, acc);
+      }
+      // force to the parent frame: (Rr n + t × Rr f, Rr f)
+      M3<R> RrR;
+      V tr;
+      load_xf(c, b, RrR, tr);
+      const SV<R> fp = force_to_parent(RrR, tr, pa);
+      store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
+    }
+  }
+  // ---- pass 3 (outward): accelerations -------------------------------------
+  SV<R> ap_{zero, zero};
+  for (int b = 0; b < c.nb; ++b) {
+    const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
+    const int type = w0 & 15, parent = (w0 >> 4) & 255, vo = (w0 >> 22) & 1023;
+    const int tb = TOPO_D * b;
+    SV<R> a;
+    if (parent == 0) {
+      a = {zero, {R(0), R(0), R(GRAVITY)}};  // inverse gravity (src/dynamics.rs:211-218)
+    } else if (parent == b) {
+      a = ap_;
+    } else {
+      a = load_sv(c, c.L.V + 6 * (parent - 1));  // pass 3 reuses V for branch accelerations
+    }
+    M3<R> Rr;
+    V t;
+    load_xf(c, b, Rr, t);
+    // a' = X a_p + c
+    a.v = mulT(Rr, a.v + cross(a.w, t));
+    a.w = mulT(Rr, a.w);
+    a = a + load_sv(c, c.L.A + 6 * b);
+    const int du = c.L.DU + DU_D * vo;
+    if (type == 1 || type == 2) {
+      const double aw[3] = {double(a.w.x), double(a.w.y), double(a.w.z)};
+      const double av[3] = {double(a.v.x), double(a.v.y), double(a.v.z)};
+      double ua = 0.0;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) ua += c.d(du + i) * aw[i] + c.d(du + 3 + i) * av[i];
+      const double x = c.d(du + 6) * (c.d(du + 7) - ua);
+      qdd[vo] = x;
+      if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
+      const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
+      if (type == 1) a.w = a.w + ax * R(x);
+      else a.v = a.v + ax * R(x);
+    } else if (type == 3) {
+      // q̈ = D⁻¹ (u − Uᵀ a') with U = D = I^A, i.e. D⁻¹ u − a'; then a = D⁻¹ u
+      double x[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) x[k] = c.d(du + 27 + k);
+      double L[21], dinv[6];
+#pragma unroll
+      for (int k = 0; k < 21; ++k) L[k] = c.d(du + k);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) dinv[k] = c.d(du + 21 + k);
+      solve6(L, dinv, x);
+      const double a6[6] = {double(a.w.x), double(a.w.y), double(a.w.z), double(a.v.x), double(a.v.y), double(a.v.z)};
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const double y = x[k] - a6[k];
+        qdd[vo + k] = y;
+        if (!isfinite(y)) st |= 1;
+      }
+      a = {{R(x[0]), R(x[1]), R(x[2])}, {R(x[3]), R(x[4]), R(x[5])}};
+    }
+    if ((w1 & 255) & BF_BRANCH) store_sv(c, c.L.V + 6 * b, a);
+    ap_ = a;
+  }
+  return st;
+}

@@ -332,6 +332,14 @@ extern "C" int gpb_batch_set_mapping(gpb_batch* b, int lanes) {
   return GPB_OK;
 }
 
+extern "C" int gpb_batch_set_algorithm(gpb_batch* b, int algorithm) {
+  if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_algorithm: batch is NULL");
+  if (algorithm != GPB_ALGO_CRBA && algorithm != GPB_ALGO_ABA)
+    return fail(GPB_E_INVAL, "gpb_batch_set_algorithm: GPB_ALGO_CRBA or GPB_ALGO_ABA");
+  b->algorithm = algorithm;
+  return GPB_OK;
+}
+
 extern "C" int gpb_batch_set_coop(gpb_batch* b, int min_dof) {
   if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_coop: batch is NULL");
   if (min_dof < -1 || min_dof > GPB_MAX_DOF)
@@ -343,7 +351,7 @@ extern "C" int gpb_batch_set_coop(gpb_batch* b, int min_dof) {
 // Packs at the front of the queue whose every instance has at least the
 // block-cooperative threshold of DOF (packs are sorted by DOF, largest first).
 static int32_t coop_packs(const gpb_batch* b, int precision) {
-  if (precision == GPB_MIXED_REFINED) return 0;
+  if (precision == GPB_MIXED_REFINED || b->algorithm != GPB_ALGO_CRBA) return 0;
   int thr = b->coop_min_dof < 0 ? kDefaultCoopMinDof : b->coop_min_dof;
   if (thr <= 0) return 0;
   if (precision == GPB_MIXED) thr = std::max(thr, 13);  // the FP64-factor form of GPB_MIXED

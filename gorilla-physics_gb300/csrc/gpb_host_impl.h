@@ -198,6 +198,7 @@ struct gpb_batch {
   int mapping = 0;
   int warps_per_sm = 0;  // resident warps per SM of the step kernel (0 = occupancy limit)
   int coop_min_dof = -1; // block-cooperative packs: DOF threshold (-1 = default, 0 = off)
+  int algorithm = GPB_ALGO_CRBA;
   std::vector<int64_t> q_off, v_off, c_off;  // user layout, [n+1]
   int64_t nq_total = 0, nv_total = 0, nc_total = 0;
   std::vector<gpb::PackDesc> packs_h;
@@ -237,6 +238,7 @@ struct gpb_batch {
     b.nv_total = nv_total;
     b.nc_total = nc_total;
     b.queue = queue.p;
+    b.algorithm = algorithm;
     return b;
   }
   void release() {

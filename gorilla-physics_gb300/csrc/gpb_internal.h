@@ -47,7 +47,7 @@ struct PackDesc {
 // Scratch sub-array offsets (rows of 8-byte words; R-typed arrays use the same
 // row pitch so that the float and double kernels share one layout).
 struct ScratchLayout {
-  int32_t X, V, A, S, I, F, C, M, D, rhs, q0, v0, qs, vs, facc, tau, cf, total;
+  int32_t X, V, A, S, I, F, C, AI, DU, RF, M, D, rhs, q0, v0, qs, vs, facc, tau, cf, total;
 };
 __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, int nc) {
   ScratchLayout s;
@@ -59,6 +59,9 @@ __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, 
   s.I = o; o += 12 * nb;  // world inertia (10) or, in link coordinates, (Rrel, t) (12)
   s.F = o; o += 6 * nb;
   s.C = o; o += 10 * nb;  // link coordinates: composite inertia accumulated from branches
+  s.AI = o; o += 21 * nb; // articulated-body algorithm: articulated inertias (FP64)
+  s.DU = o; o += 11 * nv; // articulated-body algorithm: U, 1/D, u per DOF (FP64)
+  s.RF = o; o += 12 * nb; // articulated-body algorithm: (Rrel, t) in the sweep precision
   const int nT = (nv + 3) / 4;  // mass matrix in 4x4 tiles, n padded to 4 nT
   s.M = o; o += nT * (nT + 1) / 2 * 16;
   s.D = o; o += 4 * nT;
@@ -117,6 +120,7 @@ struct DeviceBatch {
   const int64_t* cmap;     // contact slot (3 per contact) -> flat user index
   int64_t nq_total, nv_total, nc_total;
   int32_t* queue;          // persistent-kernel work counters: [0] per-warp packs, [1] block packs
+  int32_t algorithm;       // GPB_ALGO_CRBA or GPB_ALGO_ABA
   // serving pool only (all null for a batch)
   LaneJob* jobs;           // per-slot jobs
   const int32_t* active;   // packs to run in this launch (nactive of them)

@@ -72,12 +72,18 @@ struct LaneCtx {
   const int32_t* CI;  // contact ints
   const R* CD;        // contact reals
   const R* HD;        // half-space reals
+  const double* TDD;  // the same tables in FP64 (for the FP64 parts of mixed forms)
+  const double* CDD;
+  const double* HDD;
   ScratchLayout L;
   R* sR;              // scratch viewed as R (row pitch = LANES * 8 bytes)
   double* sD;         // scratch viewed as double
   char* s0;           // scratch row 0, lane 0
   __device__ __forceinline__ uint32_t w(int e) const { return W[(size_t)e * LANES]; }
   __device__ __forceinline__ R t(int e) const { return T[(size_t)e * LANES]; }
+  __device__ __forceinline__ double td(int e) const { return TDD[(size_t)e * LANES]; }
+  __device__ __forceinline__ double cdd(int e) const { return CDD[(size_t)e * LANES]; }
+  __device__ __forceinline__ double hdd(int e) const { return HDD[(size_t)e * LANES]; }
   // R-typed scratch element (e in rows of 8-byte words)
   __device__ __forceinline__ R& r(int e) const {
     return *reinterpret_cast<R*>(reinterpret_cast<char*>(sR) + (size_t)e * LANES * 8);
@@ -683,6 +689,7 @@ __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Co
 }
 
 #include "gpb_link.cuh"
+#include "gpb_aba.cuh"
 
 // MIXED_REFINED: the link-coordinate sweep in FP32 (bias forces, mass matrix,
 // Cholesky) gives x0; iterative refinement then solves H δ = τ − ID(q, q̇, x0)
@@ -774,15 +781,19 @@ __device__ __forceinline__ void advance_q(const LaneCtx<R>& c, Col<double> q, Co
 // Dynamics evaluators of the three precision modes (q, v, τ → q̈).
 struct EvalFP64 {
   LaneCtx<double> c;
+  int algo;  // GPB_ALGO_CRBA / GPB_ALGO_ABA
   __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
                             Col<double> cf = Col<double>{nullptr}, bool want_cf = false) const {
+    if (algo == 1) return lane_aba<double>(c, q, v, t, ht, x, cf, want_cf);
     return lane_dynamics<double, double>(c, q, v, t, ht, x, cf, want_cf);
   }
 };
-struct EvalMixed {  // FP32 sweeps and fill; FP64 Cholesky when n > 12
+struct EvalMixed {  // CRBA: FP32 sweeps and fill, FP64 Cholesky when n > 12; ABA: FP64 articulated inertias
   LaneCtx<float> c;
+  int algo;
   __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
                             Col<double> cf = Col<double>{nullptr}, bool want_cf = false) const {
+    if (algo == 1) return lane_aba<float>(c, q, v, t, ht, x, cf, want_cf);
     if (c.nv <= 12) return lane_dynamics<float, float>(c, q, v, t, ht, x, cf, want_cf);
     return lane_dynamics<float, double>(c, q, v, t, ht, x, cf, want_cf);
   }
@@ -873,6 +884,9 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   c.CI = b.ctcI + pd.ctc * LANES + lane;
   c.CD = RealTopo<R>::ctc(b) + pd.ctc * CTC_D * LANES + lane;
   c.HD = RealTopo<R>::hs(b) + pd.hs * HS_D * LANES + lane;
+  c.TDD = b.topoD + pd.topo * TOPO_D * LANES + lane;
+  c.CDD = b.ctcD + pd.ctc * CTC_D * LANES + lane;
+  c.HDD = b.hsD + pd.hs * HS_D * LANES + lane;
   c.L = scratch_layout(pd.nb, pd.nq, pd.nv, pd.nc);
   c.sD = b.scratch + pd.scr * LANES + lane;
   c.sR = reinterpret_cast<R*>(b.scratch + pd.scr * LANES) + lane;
@@ -911,13 +925,13 @@ struct EvalOf;
 template <>
 struct EvalOf<0> {
   __device__ static EvalFP64 make(const DeviceBatch& b, const PackDesc& pd, int lane) {
-    return EvalFP64{make_ctx<double>(b, pd, lane)};
+    return EvalFP64{make_ctx<double>(b, pd, lane), b.algorithm};
   }
 };
 template <>
 struct EvalOf<1> {
   __device__ static EvalMixed make(const DeviceBatch& b, const PackDesc& pd, int lane) {
-    return EvalMixed{make_ctx<float>(b, pd, lane)};
+    return EvalMixed{make_ctx<float>(b, pd, lane), b.algorithm};
   }
 };
 template <>

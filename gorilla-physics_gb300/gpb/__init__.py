@@ -5,7 +5,7 @@ All arithmetic runs in the CUDA kernels of libgpb.so (sm_103a); this package
 only describes mechanisms and calls the C ABI of include/gpb.h.
 """
 
-from ._abi import (FIXED, FLOATING, FP64, HUNT_CROSSLEY, LINEAR_SPRING_DAMPER, MIXED, MIXED_REFINED, PRISMATIC,
+from ._abi import (ALGO_ABA, ALGO_CRBA, FIXED, FLOATING, FP64, HUNT_CROSSLEY, LINEAR_SPRING_DAMPER, MIXED, MIXED_REFINED, PRISMATIC,
                    REVOLUTE, RUNGE_KUTTA_2, RUNGE_KUTTA_4, SEMI_IMPLICIT_EULER, GpbError, lib)
 from .batch import Batch, Context, Integrator, Precision, simulate, simulate_steps
 from .serve import Server, SlotClass
@@ -19,5 +19,5 @@ __all__ = [
     "RevoluteJoint", "PrismaticJoint", "FloatingJoint", "FixedJoint", "WORLD_FRAME", "GpbError",
     "lib", "FIXED", "REVOLUTE", "PRISMATIC", "FLOATING", "SEMI_IMPLICIT_EULER", "RUNGE_KUTTA_2",
     "RUNGE_KUTTA_4", "FP64", "MIXED", "MIXED_REFINED", "HUNT_CROSSLEY", "LINEAR_SPRING_DAMPER",
-    "Server", "SlotClass",
+    "Server", "SlotClass", "ALGO_CRBA", "ALGO_ABA",
 ]

@@ -18,6 +18,7 @@ GPB_ST_NONFINITE, GPB_ST_CHOL_FAIL = 1, 2
 FIXED, REVOLUTE, PRISMATIC, FLOATING = 0, 1, 2, 3
 SEMI_IMPLICIT_EULER, RUNGE_KUTTA_2, RUNGE_KUTTA_4 = 0, 1, 2
 FP64, MIXED, MIXED_REFINED = 0, 1, 2
+ALGO_CRBA, ALGO_ABA = 0, 1
 HUNT_CROSSLEY, LINEAR_SPRING_DAMPER = 0, 1
 CONTROL_HOST_TAU, CONTROL_OPEN_LOOP, CONTROL_PD = 0, 1, 2
 MAX_BODIES = MAX_DOF = MAX_CONTACTS = 64
@@ -125,6 +126,7 @@ SIGNATURES = [
     ("gpb_batch_set_mapping", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_batch_set_launch", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_batch_set_coop", C.c_int, [C.c_void_p, C.c_int]),
+    ("gpb_batch_set_algorithm", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_batch_autotune", C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_int, C.POINTER(GpbControl), C.c_int,
                                      P_i32, P_i32]),
     ("gpb_launch_count", C.c_int64, [C.c_void_p]),

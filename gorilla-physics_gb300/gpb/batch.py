@@ -155,6 +155,10 @@ class Batch:
         _abi.check(_abi.lib().gpb_batch_set_mapping(self.h, lanes_per_instance),
                    "gpb_batch_set_mapping")
 
+    def set_algorithm(self, algorithm: int) -> None:
+        """ALGO_CRBA (the reference's route, default) or ALGO_ABA (articulated-body algorithm)."""
+        _abi.check(_abi.lib().gpb_batch_set_algorithm(self.h, algorithm), "gpb_batch_set_algorithm")
+
     def set_coop(self, min_dof: int) -> None:
         """Block-cooperative packs from `min_dof` DOF up (-1 default, 0 off)."""
         _abi.check(_abi.lib().gpb_batch_set_coop(self.h, min_dof), "gpb_batch_set_coop")

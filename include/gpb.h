@@ -83,6 +83,17 @@ enum gpb_integrator {
  * exceeds 1e-4 of max(|q̈|, 1)); FP64 position/quaternion accumulator. */
 enum gpb_precision { GPB_FP64 = 0, GPB_MIXED = 1, GPB_MIXED_REFINED = 2 };
 
+/* How q̈ is obtained from the dynamics (gpb_batch_set_algorithm).
+ * GPB_ALGO_CRBA: the reference's route (src/dynamics.rs:322-364): RNEA bias,
+ *   CRBA mass matrix (src/mechanism.rs:592-696), then a Cholesky solve where the
+ *   reference uses LU.  The default.
+ * GPB_ALGO_ABA: Featherstone's articulated-body algorithm in link coordinates,
+ *   O(n) per instance; the same q̈ in exact arithmetic (FP64 results agree with
+ *   CRBA to the conditioning bound).  With GPB_MIXED its articulated inertias
+ *   stay in FP64 and everything else runs in FP32.  GPB_MIXED_REFINED always
+ *   uses CRBA. */
+enum gpb_algorithm { GPB_ALGO_CRBA = 0, GPB_ALGO_ABA = 1 };
+
 /* GPB_HUNT_CROSSLEY: src/contact.rs:260-338 (k = k_p k_h/(k_p+k_h), k_h = 50e3,
  * π = max(λ z^1.5 ż + k z^1.5, 0), λ = 1.5 α k).
  * GPB_LINEAR_SPRING_DAMPER: π = max(k z + c ż, 0) with the same friction. */
@@ -277,6 +288,9 @@ int gpb_batch_set_launch(gpb_batch* batch, int warps_per_sm);
  * shortens the critical path of a batch with a wide size range.  -1 = the
  * library's default, 0 = off.  Not used by GPB_MIXED_REFINED. */
 int gpb_batch_set_coop(gpb_batch* batch, int min_dof);
+
+/* GPB_ALGO_CRBA (default) or GPB_ALGO_ABA for every later dynamics call. */
+int gpb_batch_set_algorithm(gpb_batch* batch, int algorithm);
 
 /* Autotuner: times `trial_steps` steps of this batch (its own mechanisms,
  * state, step size, integrator, precision and control law) for each launch

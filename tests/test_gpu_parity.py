@@ -13,6 +13,7 @@ Tolerances
 """
 
 import math
+import sys
 
 import numpy as np
 import pytest
@@ -24,6 +25,23 @@ from tests.golden import kats
 
 pytestmark = pytest.mark.gpu
 G = 9.81
+
+
+@pytest.fixture(autouse=True, params=["crba", "aba"])
+def algorithm(request, monkeypatch):
+    """Every parity test runs with both routes to q̈: the reference's CRBA +
+    solve and the articulated-body algorithm (same bounds)."""
+    if request.param == "aba" and "refined" in request.node.name:
+        pytest.skip("MIXED_REFINED always uses CRBA")
+    algo = {"crba": gpb.ALGO_CRBA, "aba": gpb.ALGO_ABA}[request.param]
+
+    class AlgoBatch(gpb.Batch):
+        def __init__(self, *a, **k):
+            super().__init__(*a, **k)
+            self.set_algorithm(algo)
+
+    monkeypatch.setattr(sys.modules[__name__], "Batch", AlgoBatch)
+    return request.param
 
 
 def rel_err(a, b):
@@ -95,6 +113,31 @@ def test_config_dynamics_fp64(ctx, config, n, model):
     if config in (2, 3):
         assert active > n // 4
     assert np.all(B.status() == 0)
+
+
+@pytest.mark.parametrize("config,n,model", [(0, 256, 1), (1, 1024, 1), (2, 256, 1), (2, 256, 0),
+                                            (3, 128, 1), (3, 128, 0)])
+def test_mixed_aba_error_bound(ctx, algorithm, config, n, model):
+    """MIXED with the articulated-body algorithm (FP64 articulated inertias,
+    FP32 elsewhere): q̈ within 1e-5 of FP64 (relative to max(|q̈|, 1)) on at
+    least 99 % of instances, and within 1e-4 on all of them."""
+    if algorithm != "aba":
+        pytest.skip("the bound is a property of the ABA form of MIXED")
+    M, q0, v0, _ = Model.from_config(config, n, seed=13, contact_model=model)
+    qo, vo, _ = M.offsets()
+    rng = np.random.default_rng(config + 3)
+    if config in (2, 3):
+        q0 = q0.copy()
+        for i in range(n):
+            q0[qo[i] + 6] = rng.uniform(0.0, 0.4) if config == 2 else rng.uniform(0.38, 0.45)
+    tau = rng.normal(size=v0.size)
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    a = B.dynamics_continuous(tau, precision=gpb.FP64)
+    b = B.dynamics_continuous(tau, precision=gpb.MIXED)
+    errs = np.array([rel_err(b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]) for i in range(M.n)])
+    assert np.mean(errs <= 1e-5) >= 0.99, (np.mean(errs <= 1e-5), np.quantile(errs, 0.99))
+    assert errs.max() <= 1e-4, errs.max()
 
 
 def test_mixed_precision_error(ctx):
