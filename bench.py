@@ -5,8 +5,11 @@ principal axes, l ~ U(0.2, 1) m, m ~ U(0.5, 2) kg, rod inertias,
 q0 ~ U(−π, π), v0 ~ N(0, 1), open-loop τ ~ N(0, 1) resampled every 10 steps,
 semi-implicit Euler at dt = 5e-4.  One bench "step" is one integrator step of
 every instance; the timed region runs `--steps` of them in one persistent
-launch.  The line reports the mixed-precision throughput as `value`, the plain
-FP64 form beside it, and the per-step q̈ error of mixed against FP64.
+launch.  Four forms are timed: FP64 through the reference's route (CRBA +
+solve), FP64 articulated-body algorithm, mixed precision (articulated-body
+algorithm with FP64 articulated inertias) and CRBA with FP64 iterative
+refinement.  `value` is the fastest form whose per-step q̈ stays within 1e-5
+of FP64 CRBA on ≥ 99 % of instances, at the initial and the final states.
 
 `--impl reference` times the CPU restatement of the reference's `simulate`
 (the Rust crate cannot be built here) on all host cores over a bounded sample
@@ -56,6 +59,7 @@ def parse():
     ap.add_argument("--serve-drain", type=float, default=150.0, help="max seconds to drain after it")
     ap.add_argument("--serve-precisions", default="mixed,fp64")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM budget of the slot pool")
+    ap.add_argument("--serve-algorithm", default="aba", choices=["aba", "crba"])
     return ap.parse_args()
 
 
@@ -213,17 +217,20 @@ def run_reference(args):
     return 0
 
 
-def qdd_error(B, gpb, precision, where):
-    """Per-instance q̈ error of `precision` against FP64 at the batch's current
-    state (the FP64 form agrees with the oracle to ≤ max(1e-10, 5e-15 cond(M)))."""
+def qdd_error(B, gpb, precision, algorithm, where):
+    """Per-instance q̈ error of (precision, algorithm) against the FP64 form of
+    the reference's route (CRBA + solve), at the batch's current state.  That
+    FP64 form agrees with the oracle to ≤ max(1e-10, 5e-15 cond(M))."""
     ok = B.status() == 0
+    B.set_algorithm(gpb.ALGO_CRBA)
     a = B.dynamics_continuous(None, precision=gpb.FP64)
+    B.set_algorithm(algorithm)
     b = B.dynamics_continuous(None, precision=precision)
     vo = B.v_offset
     err = []
     for i in np.nonzero(ok)[0]:
         x, y = b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]
-        e = np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1.0)
+        e = np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1.0) if y.size else 0.0
         err.append(e if np.isfinite(e) else np.inf)
     err = np.asarray(err)
     fin = err[np.isfinite(err)]
@@ -231,7 +238,7 @@ def qdd_error(B, gpb, precision, where):
             "p99": float(np.quantile(err, 0.99)), "median": float(np.median(err)),
             "frac_le_1e-5": float(np.mean(err <= 1e-5)), "nonfinite": int(np.sum(~np.isfinite(err))),
             "instances": int(err.size), "state": where,
-            "norm": "max|Δq̈| / max(max|q̈_fp64|, 1) per instance"}
+            "norm": "max|Δq̈| / max(max|q̈_fp64,crba|, 1) per instance"}
 
 
 def run_gpu(args):
@@ -245,14 +252,13 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     import gpb
     from gpb import Batch, Model
-    from gpb.flops import model_flops
+    from gpb.flops import aba_model_flops, model_flops
 
     L = gpb.lib()
     ctx = gpb.Context(local)
     # weak scaling: every rank owns its own instances (seed offset by rank)
     M, q0, v0, aux = Model.from_config(args.config, args.instances, seed=shard_seed(args.seed, rank))
     B = Batch(M, ctx)
-    flops_step = float(model_flops(M, 0).sum())
     kw = dict(control=CONTROL[args.config], tau=aux if args.config == 3 else None, seed=7,
               resample_every=10, sigma=1.0, kp=50.0, kd=2.0)
     dt = DT[args.config]
@@ -267,18 +273,23 @@ def run_gpu(args):
     def reduce_sum(x):
         return all_reduce(x, "sum", world, f"cuda:{local}")
 
-    inst_flops = model_flops(M, 0).astype(np.float64)
-
-    results = {}
-    precs = {"all": ["fp64", "mixed", "refined"], "fp64": ["fp64"], "mixed": ["mixed"],
+    # the four forms: (precision, algorithm, per-instance FP64 flops of one step)
+    MODES = {
+        "fp64_crba": (gpb.FP64, gpb.ALGO_CRBA, model_flops(M, 0)),
+        "fp64": (gpb.FP64, gpb.ALGO_ABA, aba_model_flops(M, False)),
+        "mixed": (gpb.MIXED, gpb.ALGO_ABA, aba_model_flops(M, True)),
+        "refined": (gpb.MIXED_REFINED, gpb.ALGO_CRBA, model_flops(M, 0)),
+    }
+    precs = {"all": list(MODES), "fp64": ["fp64_crba", "fp64"], "mixed": ["mixed"],
              "refined": ["refined"]}[args.precision]
-    PREC = {"fp64": gpb.FP64, "mixed": gpb.MIXED, "refined": gpb.MIXED_REFINED}
+    results = {}
     launch = {}
     for name in precs:
-        prec = PREC[name]
+        prec, algo, inst_flops = MODES[name]
+        B.set_algorithm(algo)
         B.update(q0, v0)
         B.clear_status()
-        # launch shape for this workload and precision (short trials, state restored)
+        # launch shape for this workload and form (short trials, state restored)
         w, c = B.autotune(dt, 0, prec, trial_steps=10, **kw)
         launch[name] = {"warps_per_sm": w, "coop_min_dof": c}
         if args.warmup:
@@ -301,20 +312,22 @@ def run_gpu(args):
         results[name] = {"kernel_ms": kernel_ms, "wall_s": wall, "clocks": clk.summary(),
                          "failed_instances": bad, "launches": timed_launches,
                          "done": reduce_sum(float(done.sum())),
-                         "flops": reduce_sum(float(np.dot(done, inst_flops)))}
-    # q̈ error of the reduced-precision modes against FP64, at the final state of
-    # the last timed run and at the configuration's initial states
+                         "flops": reduce_sum(float(np.dot(done, inst_flops.astype(np.float64))))}
+    # q̈ error of every form against FP64 CRBA, at the final state of the last
+    # timed run and at the configuration's initial states
     errs = {}
-    for name in [p for p in precs if p != "fp64"]:
-        errs[name] = {"final": qdd_error(B, gpb, PREC[name], f"after the {args.steps}-step "
-                                                             f"timed run ({precs[-1]})")}
+    for name in [p for p in precs if p != "fp64_crba"]:
+        prec, algo, _ = MODES[name]
+        errs[name] = {"final": qdd_error(B, gpb, prec, algo, f"after the {args.steps}-step timed run ({precs[-1]})")}
     B.update(q0, v0)
     B.clear_status()
     for name in errs:
-        errs[name]["initial"] = qdd_error(B, gpb, PREC[name], "the configuration's initial states")
-    # headline: the fastest mode that meets the stated bound (≤ 1e-5 on ≥ 99 % of
-    # instances at both states), else FP64
-    head_name = "fp64" if "fp64" in results else precs[0]
+        prec, algo, _ = MODES[name]
+        errs[name]["initial"] = qdd_error(B, gpb, prec, algo, "the configuration's initial states")
+    # headline: the fastest form that meets the stated bound (≤ 1e-5 on ≥ 99 % of
+    # instances at both states); the FP64 forms are exact to round-off
+    head_name = max([p for p in precs if p.startswith("fp64")] or precs[:1],
+                    key=lambda n: results[n]["done"] / results[n]["kernel_ms"])
     for name in ["mixed", "refined"]:
         e = errs.get(name)
         if name in results and e and all(x["frac_le_1e-5"] >= 0.99 for x in e.values()):
@@ -324,7 +337,8 @@ def run_gpu(args):
     q_h = torch.from_numpy(q0).pin_memory()
     v_h = torch.from_numpy(v0).pin_memory()
     qn, vn = q_h.numpy(), v_h.numpy()
-    prec = PREC[head_name]
+    prec, algo, _ = MODES[head_name]
+    B.set_algorithm(algo)
     barrier()
     ctx.synchronize()
     t0 = time.perf_counter()
@@ -345,41 +359,49 @@ def run_gpu(args):
 
     p64, p32 = peak(gpb.FP64), peak(gpb.MIXED)
 
-    def roof(res, bound, pk):
-        ach = res["flops"] / (res["kernel_ms"] * 1e-3) / 1e12
-        return {"bound": bound, "achieved": ach, "peak": pk, "unit": "TFLOP/s", "frac": ach / pk,
-                "traffic": None, "peak_source": "measured FMA microbenchmark (gpb_fma_peak), this run",
-                "work": f"{flops_step / args.instances:.0f} algorithmic flops per instance-step "
-                        f"(mean; gpb.flops); completed instance-steps only"}
+    WORK = {"fp64_crba": "CRBA + RNEA + Cholesky flops (gpb.flops.model_flops)",
+            "fp64": "articulated-body algorithm flops (gpb.flops.aba_model_flops)",
+            "mixed": "FP64 share of the mixed articulated-body algorithm (gpb.flops.aba_model_flops(mixed=True))",
+            "refined": "CRBA-equivalent flops (the FP64 residual is a part of them)"}
 
+    def roof(name, res):
+        ach = res["flops"] / (res["kernel_ms"] * 1e-3) / 1e12
+        per = res["flops"] / max(res["done"], 1.0)
+        return {"bound": "fp64", "achieved": ach, "peak": p64, "unit": "TFLOP/s", "frac": ach / p64,
+                "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (gpb_fma_peak), this run",
+                "work": f"{per:.0f} FP64 flops per completed instance-step (mean): {WORK[name]}"}
+
+    DTYPE = {"fp64_crba": "f64", "fp64": "f64",
+             "mixed": "f32 kinematics/bias + f64 articulated inertias + f64 state",
+             "refined": "f32 solve + f64 residual refinement + f64 state"}
+    ALGO = {"fp64_crba": "CRBA + Cholesky (the reference's route)", "fp64": "articulated-body algorithm",
+            "mixed": "articulated-body algorithm", "refined": "CRBA + Cholesky, iterative refinement"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["kernel_ms"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp64": "f64", "mixed": "f32 sweeps + f64 Cholesky (n>12) + f64 state",
-                  "refined": "f32 solve + f64 residual refinement + f64 state"}[head_name],
+        "dtype": DTYPE[head_name],
         "data": "synthetic (seeded Philox4x32-10 draws of the configuration's distributions)",
         "config": {"workload": f"{CONFIG_NAME[args.config]} x {args.instances} per GPU",
-                   "precision_mode": head_name,
+                   "precision_mode": head_name, "algorithm": ALGO[head_name],
                    "dof": "U{2..48}" if args.config == 1 else None, "dt": dt,
                    "integrator": "semi-implicit Euler", "control": CONTROL[args.config],
                    "l2": "inputs larger than L2 (topology + state + scratch > 129 MB)"},
         "gpu_launches": head["launches"],
     }
-    bound = {"fp64": ("fp64", p64), "mixed": ("fp32", p32), "refined": ("fp32", p32)}
     line["modes"] = {}
     for name, r in results.items():
         line["modes"][name] = {
             "value": r["done"] / (r["kernel_ms"] * 1e-3), "ms_per_step": r["kernel_ms"] / args.steps,
-            "roofline": roof(r, *bound[name]),
+            "algorithm": ALGO[name], "dtype": DTYPE[name], "roofline": roof(name, r),
             "launch": launch.get(name),
-            "qdd_rel_err_vs_fp64": errs.get(name)}
-    if "fp64" in results:
-        line["fp64"] = line["modes"]["fp64"]
-        for name in ("mixed", "refined"):
-            if name in results:
-                line[f"{name}_over_fp64"] = line["modes"][name]["value"] / line["fp64"]["value"]
-    line["roofline"] = roof(head, *bound[head_name])
+            "qdd_rel_err_vs_fp64_crba": errs.get(name)}
+    for base in ("fp64", "fp64_crba"):
+        if base in results:
+            for name in ("mixed", "refined", "fp64"):
+                if name in results and name != base:
+                    line[f"{name}_over_{base}"] = line["modes"][name]["value"] / line["modes"][base]["value"]
+    line["roofline"] = roof(head_name, head)
     line["peaks_measured"] = {"fp64_tflops": p64, "fp32_tflops": p32}
     line["clocks"] = head["clocks"]
     line["failed_instances"] = {k: r["failed_instances"] for k, r in results.items()}
@@ -460,7 +482,8 @@ def run_serve(args):
                 per.append({"idx": idx, "M": M, "q0": q0, "v0": v0, "aux": aux, "next": 0,
                             "t": t_arr[idx]})
             S = Server(ctx, serve_classes(int(args.serve_budget_gb * 1e9)), precision=prec_of[pname],
-                       chunk_steps=16, hbm_budget_bytes=int(args.serve_budget_gb * 1e9))
+                       chunk_steps=16, hbm_budget_bytes=int(args.serve_budget_gb * 1e9),
+                       algorithm=gpb.ALGO_ABA if args.serve_algorithm == "aba" else gpb.ALGO_CRBA)
             req_of = {}
             lat = np.full(n, np.nan)
             steps_done_total = 0

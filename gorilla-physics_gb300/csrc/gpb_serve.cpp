@@ -200,6 +200,8 @@ extern "C" int gpb_server_create(gpb_ctx* ctx, const gpb_server_opts* o, gpb_ser
   if (o->precision != GPB_FP64 && o->precision != GPB_MIXED && o->precision != GPB_MIXED_REFINED)
     return fail(GPB_E_INVAL, "gpb_server_create: unknown precision");
   if (o->chunk_steps < 1) return fail(GPB_E_INVAL, "gpb_server_create: chunk_steps must be >= 1");
+  if (o->algorithm != GPB_ALGO_CRBA && o->algorithm != GPB_ALGO_ABA)
+    return fail(GPB_E_INVAL, "gpb_server_create: unknown algorithm");
   std::vector<int32_t> np(o->n_classes > 0 && o->n_classes <= 16 ? o->n_classes : 1);
   std::vector<int64_t> pb(np.size());
   if (int r = gpb_server_plan(o, np.data(), pb.data())) return r;
@@ -226,6 +228,7 @@ extern "C" int gpb_server_create(gpb_ctx* ctx, const gpb_server_opts* o, gpb_ser
   // pack descriptors: capacities of the class, rows laid out pack after pack
   gpb_batch& B = S->pool;
   B.ctx = ctx;
+  B.algorithm = o->algorithm;
   B.npacks = npacks;
   B.packs_h.resize(npacks);
   S->pack_class.assign(npacks, 0);

@@ -81,6 +81,7 @@ class GpbServerOpts(C.Structure):
         ("n_classes", C.c_int32),
         ("classes", C.POINTER(GpbSlotClass)),
         ("max_admit_per_tick", C.c_int32),
+        ("algorithm", C.c_int32),
     ]
 
 

@@ -63,3 +63,65 @@ def model_flops(model, integrator: int = 0) -> np.ndarray:
             cache[key] = instance_flops(t, p, key[2])
         out[i] = evals * cache[key]
     return out
+
+
+# ---------------------------------------------------------------------------
+# Articulated-body algorithm (GPB_ALGO_ABA), counted from its three passes as
+# implemented (same convention).  Per body, FP64 form:
+#   revolute about a principal axis with identity init rotation  620
+#     (pass 1: sin/cos 2, transforms 42, bias acceleration 30, v ×* I v 72;
+#      pass 2: U, D, u 13, I^A − U D⁻¹ Uᵀ 48, I^a c + U D⁻¹ u 84, congruence to
+#      the parent 183 (planar rotation 84, shift 99), accumulation 21, force to
+#      the parent 48; pass 3: 67)
+#   other revolute 845, prismatic 800 (full 3×3 rotation of the congruence,
+#   Rodrigues, U = I^A S with a general axis), floating root 440 (6×6
+#   Cholesky and solve), fixed 650
+#   contact point 130, plus 60 per body of a mechanism with contacts (FP64
+#   world poses)
+# GPB_MIXED keeps in FP64 only U, D, the articulated-inertia update, the
+# congruence and accumulation, the final q̈ dot products and everything that
+# places contacts: 275 per planar revolute body, 460 other revolute, 440
+# prismatic, 240 floating root, 380 fixed; contacts as above.
+# ---------------------------------------------------------------------------
+
+ABA_FP64 = {"rev_planar": 620, "rev": 845, "pri": 800, "float": 440, "fixed": 650}
+ABA_MIXED_FP64 = {"rev_planar": 275, "rev": 460, "pri": 440, "float": 240, "fixed": 380}
+ABA_CONTACT = 130
+ABA_POSE = 60
+
+
+def _aba_kinds(model, i):
+    jo = model.joint_offset
+    kinds = []
+    for j in range(jo[i], jo[i + 1]):
+        t = int(model.joint_type[j])
+        if t == 1:
+            iso = model.joint_iso[7 * j:7 * j + 4]
+            ax = model.joint_axis[3 * j:3 * j + 3]
+            planar = (iso[0] == 0 and iso[1] == 0 and iso[2] == 0 and iso[3] == 1 and
+                      np.count_nonzero(ax) == 1 and abs(ax[np.nonzero(ax)[0][0]]) == 1.0)
+            kinds.append("rev_planar" if planar else "rev")
+        else:
+            kinds.append({0: "fixed", 2: "pri", 3: "float"}[t])
+    return kinds
+
+
+def aba_model_flops(model, mixed: bool = False, integrator: int = 0) -> np.ndarray:
+    """Per-instance FP64 flops of one integrator step with the articulated-body
+    algorithm (all of it for GPB_FP64; the FP64 share for GPB_MIXED)."""
+    evals = {0: 1, 1: 2, 2: 4}[integrator]
+    table = ABA_MIXED_FP64 if mixed else ABA_FP64
+    out = np.zeros(model.n, np.int64)
+    co = model.contact_offset
+    cache: dict = {}
+    for i in range(model.n):
+        kinds = tuple(_aba_kinds(model, i))
+        nc = int(co[i + 1] - co[i])
+        key = (kinds, nc)
+        if key not in cache:
+            f = sum(table[k] for k in kinds)
+            if nc:
+                f += ABA_CONTACT * nc + ABA_POSE * len(kinds)
+            cache[key] = f
+        out[i] = evals * cache[key]
+    return out

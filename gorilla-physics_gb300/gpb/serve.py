@@ -45,10 +45,10 @@ REQUEST_DTYPE = np.dtype([("dt", "f8"), ("steps", "i8"), ("integrator", "i4"), (
 assert REQUEST_DTYPE.itemsize == C.sizeof(_abi.GpbRequest)
 
 
-def _opts(classes, precision, chunk_steps, hbm_budget_bytes, max_admit_per_tick):
+def _opts(classes, precision, chunk_steps, hbm_budget_bytes, max_admit_per_tick, algorithm=_abi.ALGO_CRBA):
     arr = (_abi.GpbSlotClass * len(classes))(*[c.struct() for c in classes])
     o = _abi.GpbServerOpts(precision, chunk_steps, int(hbm_budget_bytes), len(classes),
-                           C.cast(arr, C.POINTER(_abi.GpbSlotClass)), max_admit_per_tick)
+                           C.cast(arr, C.POINTER(_abi.GpbSlotClass)), max_admit_per_tick, algorithm)
     return o, arr
 
 
@@ -65,9 +65,9 @@ def plan(classes, hbm_budget_bytes: int = 0, precision: int = _abi.MIXED, chunk_
 
 class Server:
     def __init__(self, ctx: Context, classes, precision: int = _abi.MIXED, chunk_steps: int = 64,
-                 hbm_budget_bytes: int = 0, max_admit_per_tick: int = 0):
+                 hbm_budget_bytes: int = 0, max_admit_per_tick: int = 0, algorithm: int = _abi.ALGO_CRBA):
         self.ctx = ctx
-        o, keep = _opts(classes, precision, chunk_steps, hbm_budget_bytes, max_admit_per_tick)
+        o, keep = _opts(classes, precision, chunk_steps, hbm_budget_bytes, max_admit_per_tick, algorithm)
         h = C.c_void_p()
         _abi.check(_abi.lib().gpb_server_create(ctx.h, C.byref(o), C.byref(h)), "gpb_server_create")
         self.h = h

@@ -371,6 +371,7 @@ typedef struct gpb_server_opts {
   int32_t n_classes;          /* 1..16 */
   const gpb_slot_class* classes;
   int32_t max_admit_per_tick; /* 0 = no limit */
+  int32_t algorithm;          /* GPB_ALGO_CRBA or GPB_ALGO_ABA */
 } gpb_server_opts;
 
 typedef struct gpb_request {
