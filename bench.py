@@ -428,13 +428,15 @@ SERVE_MIX = (0.4, 0.3, 0.2, 0.1)
 SERVE_HORIZON = (100, 50000)
 
 
-def serve_classes(budget_bytes):
+def serve_classes(budget_bytes, algorithm="aba"):
     """Slot classes of the serving mix (chains split by DOF), budget shares by
     expected occupancy (mix share × mean per-step cost), and per-class chunk
     steps that make one tick cost about the same for every class."""
     from gpb.serve import SlotClass
 
-    def cost(nb, nv, nc):  # algorithmic flops per step (leading terms)
+    def cost(nb, nv, nc):  # FP64 flops per step (leading terms of gpb.flops)
+        if algorithm == "aba":
+            return 620 * nb + 130 * nc + (60 * nb if nc else 0)
         return 625 * nb + 11 * nv * (nv + 1) / 2 + nv ** 3 / 3 + 2 * nv * nv + 80 * nc
 
     specs = [((2, 2, 2, 0, 0), SERVE_MIX[0])]
@@ -481,7 +483,8 @@ def run_serve(args):
                 M, q0, v0, aux = Model.from_config(c, max(len(idx), 1), seed=args.seed + 17 * c)
                 per.append({"idx": idx, "M": M, "q0": q0, "v0": v0, "aux": aux, "next": 0,
                             "t": t_arr[idx]})
-            S = Server(ctx, serve_classes(int(args.serve_budget_gb * 1e9)), precision=prec_of[pname],
+            S = Server(ctx, serve_classes(int(args.serve_budget_gb * 1e9), args.serve_algorithm),
+                       precision=prec_of[pname],
                        chunk_steps=16, hbm_budget_bytes=int(args.serve_budget_gb * 1e9),
                        algorithm=gpb.ALGO_ABA if args.serve_algorithm == "aba" else gpb.ALGO_CRBA)
             req_of = {}

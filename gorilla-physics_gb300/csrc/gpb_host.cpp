@@ -545,7 +545,8 @@ extern "C" int gpb_batch_autotune(gpb_batch* b, double dt, int integrator, int p
   std::vector<std::pair<int, int>> cand;
   for (int w : {4, 8}) {
     cand.push_back({w, 0});
-    if (precision != GPB_MIXED_REFINED && b->npacks > 0 && b->packs_h[0].minnv >= 32)
+    if (precision != GPB_MIXED_REFINED && b->algorithm == GPB_ALGO_CRBA && b->npacks > 0 &&
+        b->packs_h[0].minnv >= 32)
       for (int c : {40, 32}) cand.push_back({w, c});
   }
   double best = 1e300;
