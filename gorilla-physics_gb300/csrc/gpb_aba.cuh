@@ -527,8 +527,8 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     }
     store_sv(c, c.L.A + 6 * b, cb);
     store_sv(c, c.L.F + 6 * b, p);
-    store_abi(c, c.L.AI + ABI_D * b, body_abi(c, tb));
     if (fl & BF_BRANCH) {
+      store_abi(c, c.L.AI + ABI_D * b, ABI{});  // accumulator for children other than b+1
       store_sv(c, c.L.V + 6 * b, vb);
       if (contacts) {
 #pragma unroll
@@ -544,13 +544,23 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     pR = Rw;
   }
   // ---- pass 2 (inward): articulated inertias and bias forces --------------
+  // A child that is the next body (every link of a chain) hands its terms to
+  // the parent in registers; other children accumulate into the parent's slot.
+  ABI carryI;
+  SV<R> carryP;
+  int ctarget = -1;
   for (int b = c.nb - 1; b >= 0; --b) {
     const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
     const uint32_t fl = w1 & 255;
     const int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
     const int tb = TOPO_D * b;
-    ABI IA = load_abi(c, c.L.AI + ABI_D * b);
-    const SV<R> pA = load_sv(c, c.L.F + 6 * b);
+    ABI IA = body_abi(c, tb);
+    SV<R> pA = load_sv(c, c.L.F + 6 * b);
+    if (fl & BF_BRANCH) abi_add(IA, load_abi(c, c.L.AI + ABI_D * b));
+    if (ctarget == b) {
+      abi_add(IA, carryI);
+      pA = pA + carryP;
+    }
     const SV<R> cb = load_sv(c, c.L.A + 6 * b);
     SV<R> pa;  // bias force handed to the parent
     const bool to_parent = parent != 0;
@@ -655,17 +665,31 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
           co = Rr[3 * i1 + i1];
           si = Rr[3 * i2 + i1];
         }
-        ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si);
-        ABI acc = load_abi(c, c.L.AI + ABI_D * pb);
-        abi_add(acc, Ip);
-        store_abi(c, c.L.AI + ABI_D * pb, acc);
+        const ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si);
+        if (pb == b - 1) {
+          carryI = Ip;
+        } else {
+          ABI acc = load_abi(c, c.L.AI + ABI_D * pb);
+          abi_add(acc, Ip);
+          store_abi(c, c.L.AI + ABI_D * pb, acc);
+        }
+      } else if (pb == b - 1) {
+        carryI = ABI{};  // floating joint below the parent: I^a = 0
       }
       // force to the parent frame: (Rr n + t × Rr f, Rr f)
       M3<R> RrR;
       V tr;
       load_xf(c, b, RrR, tr);
       const SV<R> fp = force_to_parent(RrR, tr, pa);
-      store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
+      if (pb == b - 1) {
+        carryP = fp;
+        ctarget = pb;
+      } else {
+        store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
+        ctarget = -1;
+      }
+    } else {
+      ctarget = -1;
     }
   }
   // ---- pass 3 (outward): accelerations -------------------------------------
