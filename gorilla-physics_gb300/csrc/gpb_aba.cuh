@@ -164,38 +164,74 @@ __device__ __forceinline__ void sym_pack(const double* F, double* S) {
   S[0] = F[0], S[1] = F[4], S[2] = F[8], S[3] = F[1], S[4] = F[2], S[5] = F[5];
 }
 
-// Articulated inertia of a child, in the child frame, expressed in the parent
-// frame: X*ᵀ I X for the child→parent transform (rotation Rr, child origin t).
-// Rotation of every block, then the shift by t (T = [t]×):
-//   C_p = C', B_p = B' + T C', A_p = A' − B'T − (B'T)ᵀ − T C' T.
-// `planar` ≥ 0: Rr is the rotation about principal axis `planar` by (co, si).
-__device__ __forceinline__ ABI abi_to_parent(const ABI& I, const double* Rr, V3<double> t, int planar, double co,
-                                             double si) {
-  double A[9], B[9], Cm[9];
-  if (planar >= 0) {
-    double a6[6], c6[6];
+// Rotation about principal axis K (compile-time indices) by (co, si) of the
+// three blocks, into full 3×3 arrays.
+template <int K>
+__device__ __forceinline__ void rotate_planar(const ABI& I, double co, double si, double* A, double* B, double* Cm) {
+  constexpr int i1 = (K + 1) % 3, i2 = (K + 2) % 3;
+  double a6[6], c6[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      a6[k] = I.A[k];
-      c6[k] = I.C[k];
-    }
-    sym_planar(a6, planar, co, si);
-    sym_planar(c6, planar, co, si);
-    sym_expand(a6, A);
-    sym_expand(c6, Cm);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) B[k] = I.B[k];
-    planar_rows(B, planar, co, si);
-    planar_cols(B, planar, co, si);
-  } else {
-    double a6[6], c6[6];
-    sym_rotate(Rr, I.A, a6);
-    sym_rotate(Rr, I.C, c6);
-    gen_rotate(Rr, I.B, B);
-    sym_expand(a6, A);
-    sym_expand(c6, Cm);
+  for (int k = 0; k < 6; ++k) {
+    a6[k] = I.A[k];
+    c6[k] = I.C[k];
   }
-  // T = [t]×: rows (0, −tz, ty), (tz, 0, −tx), (−ty, tx, 0)
+  sym_planar(a6, K, co, si);
+  sym_planar(c6, K, co, si);
+  sym_expand(a6, A);
+  sym_expand(c6, Cm);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) B[k] = I.B[k];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {  // rows
+    const double x = B[3 * i1 + j], y = B[3 * i2 + j];
+    B[3 * i1 + j] = co * x - si * y;
+    B[3 * i2 + j] = si * x + co * y;
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {  // columns
+    const double x = B[3 * r + i1], y = B[3 * r + i2];
+    B[3 * r + i1] = co * x - si * y;
+    B[3 * r + i2] = si * x + co * y;
+  }
+}
+
+// The shift by t = τ e_J (compile-time J): with T = τ [e_J]× only the rows /
+// columns J+1, J+2 take part —
+//   W = T C': W[j1] = −τ C'[j2], W[j2] = τ C'[j1];  B'T: column j2 = −τ B'[:, j1],
+//   column j1 = τ B'[:, j2];  T C' T: (j1,j1) = −τ² C'_j2j2, (j2,j2) = −τ² C'_j1j1,
+//   (j1,j2) = τ² C'_j1j2.
+template <int J>
+__device__ __forceinline__ void shift_axis(const double* A, const double* B, const double* Cm, double tau, ABI& o) {
+  constexpr int j1 = (J + 1) % 3, j2 = (J + 2) % 3;
+  double W[9], BT[9], TCT[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) W[k] = BT[k] = TCT[k] = 0.0;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    W[3 * j1 + m] = -tau * Cm[3 * j2 + m];
+    W[3 * j2 + m] = tau * Cm[3 * j1 + m];
+    BT[3 * m + j2] = -tau * B[3 * m + j1];
+    BT[3 * m + j1] = tau * B[3 * m + j2];
+  }
+  const double t2 = tau * tau;
+  TCT[3 * j1 + j1] = -t2 * Cm[3 * j2 + j2];
+  TCT[3 * j2 + j2] = -t2 * Cm[3 * j1 + j1];
+  TCT[3 * j1 + j2] = TCT[3 * j2 + j1] = t2 * Cm[3 * j1 + j2];
+  const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const int i = ii[k], j = jj[k];
+    o.A[k] = A[3 * i + j] - BT[3 * i + j] - BT[3 * j + i] - TCT[3 * i + j];
+    o.C[k] = Cm[3 * i + j];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) o.B[k] = B[k] + W[k];
+}
+
+// General shift by t (T = [t]×): C_p = C', B_p = B' + T C',
+// A_p = A' − B'T − (B'T)ᵀ − T C' T.
+__device__ __forceinline__ void shift_general(const double* A, const double* B, const double* Cm, V3<double> t,
+                                              ABI& o) {
   double W[9], BT[9];  // W = T C', BT = B' T
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
@@ -209,7 +245,6 @@ __device__ __forceinline__ ABI abi_to_parent(const ABI& I, const double* Rr, V3<
     BT[3 * i + 1] = -B[3 * i] * t.z + B[3 * i + 2] * t.x;
     BT[3 * i + 2] = B[3 * i] * t.y - B[3 * i + 1] * t.x;
   }
-  ABI o;
   const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
@@ -222,6 +257,79 @@ __device__ __forceinline__ ABI abi_to_parent(const ABI& I, const double* Rr, V3<
   }
 #pragma unroll
   for (int k = 0; k < 9; ++k) o.B[k] = B[k] + W[k];
+}
+
+// Articulated inertia of a child, in the child frame, expressed in the parent
+// frame: X*ᵀ I X for the child→parent transform (rotation Rr, child origin t):
+// every block rotated (R S Rᵀ), then shifted by t.  `planar` ≥ 0: Rr is the
+// rotation about that principal axis by (co, si); `taxis` ≥ 0: t lies along
+// that axis (3: t = 0).  When every active lane of the warp has the same
+// (planar, taxis) — mechanisms of one design — code with compile-time indices
+// runs; otherwise (lanes with different axes) one runtime-indexed path serves
+// all lanes without divergence.
+__device__ __forceinline__ ABI abi_to_parent(const ABI& I, const double* Rr, V3<double> t, int planar, double co,
+                                             double si, int taxis) {
+  const unsigned am = __activemask();
+  const int key = (planar + 1) * 8 + (taxis + 1);
+  const bool uniform = __all_sync(am, key == __shfl_sync(am, key, __ffs(am) - 1));
+  double A[9], B[9], Cm[9];
+  if (!uniform) {
+    if (planar >= 0) {
+      double a6[6], c6[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        a6[k] = I.A[k];
+        c6[k] = I.C[k];
+      }
+      sym_planar(a6, planar, co, si);
+      sym_planar(c6, planar, co, si);
+      sym_expand(a6, A);
+      sym_expand(c6, Cm);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) B[k] = I.B[k];
+      planar_rows(B, planar, co, si);
+      planar_cols(B, planar, co, si);
+    } else {
+      double a6[6], c6[6];
+      sym_rotate(Rr, I.A, a6);
+      sym_rotate(Rr, I.C, c6);
+      gen_rotate(Rr, I.B, B);
+      sym_expand(a6, A);
+      sym_expand(c6, Cm);
+    }
+    ABI o;
+    shift_general(A, B, Cm, t, o);
+    return o;
+  }
+  if (planar == 0) {
+    rotate_planar<0>(I, co, si, A, B, Cm);
+  } else if (planar == 1) {
+    rotate_planar<1>(I, co, si, A, B, Cm);
+  } else if (planar == 2) {
+    rotate_planar<2>(I, co, si, A, B, Cm);
+  } else {
+    double a6[6], c6[6];
+    sym_rotate(Rr, I.A, a6);
+    sym_rotate(Rr, I.C, c6);
+    gen_rotate(Rr, I.B, B);
+    sym_expand(a6, A);
+    sym_expand(c6, Cm);
+  }
+  ABI o;
+  if (taxis == 0) {
+    shift_axis<0>(A, B, Cm, t.x, o);
+  } else if (taxis == 1) {
+    shift_axis<1>(A, B, Cm, t.y, o);
+  } else if (taxis == 2) {
+    shift_axis<2>(A, B, Cm, t.z, o);
+  } else if (taxis == 3) {
+    sym_pack(A, o.A);
+    sym_pack(Cm, o.C);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) o.B[k] = B[k];
+  } else {
+    shift_general(A, B, Cm, t, o);
+  }
   return o;
 }
 
@@ -321,6 +429,28 @@ __device__ __forceinline__ void load_xf(const LaneCtx<R>& c, int b, M3<R>& Rr, V
     for (int k = 0; k < 9; ++k) Rr.a[k] = c.r(c.L.RF + 12 * b + k);
     t = {c.r(c.L.RF + 12 * b + 9), c.r(c.L.RF + 12 * b + 10), c.r(c.L.RF + 12 * b + 11)};
   }
+}
+
+template <typename R>
+__device__ __forceinline__ SV<double> sv_d(const SV<R>& s) {
+  return {{double(s.w.x), double(s.w.y), double(s.w.z)}, {double(s.v.x), double(s.v.y), double(s.v.z)}};
+}
+template <typename R>
+__device__ __forceinline__ SV<R> sv_r(const SV<double>& s) {
+  return {{R(s.w.x), R(s.w.y), R(s.w.z)}, {R(s.v.x), R(s.v.y), R(s.v.z)}};
+}
+template <typename R>
+__device__ __forceinline__ SV<double> load_svd(const LaneCtx<R>& c, int base) {
+  return {{c.d(base), c.d(base + 1), c.d(base + 2)}, {c.d(base + 3), c.d(base + 4), c.d(base + 5)}};
+}
+template <typename R>
+__device__ __forceinline__ void store_svd(const LaneCtx<R>& c, int base, const SV<double>& s) {
+  c.d(base) = s.w.x;
+  c.d(base + 1) = s.w.y;
+  c.d(base + 2) = s.w.z;
+  c.d(base + 3) = s.v.x;
+  c.d(base + 4) = s.v.y;
+  c.d(base + 5) = s.v.z;
 }
 
 // One dynamics evaluation by the articulated-body algorithm.  q̈ into qdd;
@@ -466,48 +596,69 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     I.m = c.t(tb + TD_INERTIA);
     const SV<R> vb{om, vl};
     SV<R> p = crf(vb, imul(I, vb));
+    // contact wrench (body frame), FP64: stiff contacts make it the largest term
+    // of the bias force, and the root's u = τ − p^A reads it directly
+    SV<double> wc{{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
     if (contacts) {
       posw = posw + mul(Rw, td);
       Rw = mul(Rw, Rd);
       const int cb0 = (w1 >> 8) & 255, cn = (w1 >> 16) & 255;
       if (cn) {
-        const VD omd{double(om.x), double(om.y), double(om.z)}, vld{double(vl.x), double(vl.y), double(vl.z)};
-        const VD omw = mul(Rw, omd), vw = mul(Rw, vld);
+        // Only the penetration needs FP64 (it is a small difference of O(1)
+        // positions, and k·δ becomes force); the force law, the contact
+        // velocity and the wrench run in R in the body frame (the law depends
+        // only on n·v, |v_t| and z, so it is frame-independent).
+        M3<R> RwR;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) RwR.a[k] = R(Rw.a[k]);
         for (int k = cb0; k < cb0 + cn; ++k) {
           const int cd = CTC_D * k;
-          const VD loc{c.cdd(cd), c.cdd(cd + 1), c.cdd(cd + 2)};
-          const double kp = c.cdd(cd + 3), rad = c.cdd(cd + 4), damp = c.cdd(cd + 5);
-          const VD pwc = mul(Rw, loc) + posw;
-          VD fsum{0.0, 0.0, 0.0};
+          const VD locd{c.cdd(cd), c.cdd(cd + 1), c.cdd(cd + 2)};
+          const V loc{c.CD[(size_t)cd * LANES], c.CD[(size_t)(cd + 1) * LANES], c.CD[(size_t)(cd + 2) * LANES]};
+          const R kp = c.CD[(size_t)(cd + 3) * LANES], rad = c.CD[(size_t)(cd + 4) * LANES],
+                  damp = c.CD[(size_t)(cd + 5) * LANES];
+          const double radd = c.cdd(cd + 4);
+          const VD pwc = mul(Rw, locd) + posw;
+          V fsum = zero;
           for (int h = 0; h < c.nh; ++h) {
             const int hd = HS_D * h;
             const VD hp{c.hdd(hd), c.hdd(hd + 1), c.hdd(hd + 2)};
-            const VD hn{c.hdd(hd + 3), c.hdd(hd + 4), c.hdd(hd + 5)};
-            const double alh = c.hdd(hd + 6), mu = c.hdd(hd + 7);
-            const double dist = dot(pwc - hp, hn);
-            VD app = pwc;
+            const VD hnd{c.hdd(hd + 3), c.hdd(hd + 4), c.hdd(hd + 5)};
+            const double dist = dot(pwc - hp, hnd);
             double pen;
-            if (rad > 0.0) {
-              if (!(dist - rad <= 1e-8)) continue;
-              pen = rad - dist;
-              app = pwc - hn * rad;
+            if (radd > 0.0) {
+              if (!(dist - radd <= 1e-8)) continue;
+              pen = radd - dist;
             } else {
               if (!(dist <= 1e-8)) continue;  // HalfSpace::has_inside (margin 1e-8)
               pen = -dist;
             }
-            const VD vel = vw + cross(omw, app - posw);
-            const VD fc = contact_force<double>(c.model, pen, hn, vel, kp, damp, alh, mu);
-            const VD fbd = mulT(Rw, fc), rbd = mulT(Rw, app - posw);
-            const VD nb = cross(rbd, fbd);
-            p.w = p.w - V{R(nb.x), R(nb.y), R(nb.z)};
-            p.v = p.v - V{R(fbd.x), R(fbd.y), R(fbd.z)};
-            fsum = fsum + fc;
+            const double alh = c.hdd(hd + 6), mu = c.hdd(hd + 7);
+            // The contact-point velocity v + ω × r cancels for rolling or
+            // sticking contacts, its tangential part cancels for normal impacts,
+            // and the regularised friction divides it by 1e-3: the velocity and
+            // the force law run in FP64, the wrench in R.
+            const VD nbd = mulT(Rw, hnd);  // normal in the body frame
+            const V nb{R(nbd.x), R(nbd.y), R(nbd.z)};
+            const V app = rad > R(0) ? loc - nb * rad : loc;  // application point (body frame)
+            const VD appd = radd > 0.0 ? locd - nbd * radd : locd;
+            // a floating root's body velocity is the state itself: read it unrounded
+            const bool root6 = type == 3 && parent == 0;
+            const VD vld = root6 ? VD{v[vo + 3], v[vo + 4], v[vo + 5]} : VD{double(vl.x), double(vl.y), double(vl.z)};
+            const VD omd = root6 ? VD{v[vo], v[vo + 1], v[vo + 2]} : VD{double(om.x), double(om.y), double(om.z)};
+            const VD vd = vld + cross(omd, appd);
+            const VD fbd = contact_force<double>(c.model, pen, nbd, vd, c.cdd(cd + 3), c.cdd(cd + 5), alh, mu);
+            const V fb{R(fbd.x), R(fbd.y), R(fbd.z)};
+            wc.w = wc.w - cross(appd, fbd);
+            wc.v = wc.v - fbd;
+            fsum = fsum + fb;
           }
           if (want_cf) {
+            const V fw = mul(RwR, fsum);
             const int orig = (c.CI[(size_t)k * LANES] >> 8) & 255;
-            cf[3 * orig] = fsum.x;
-            cf[3 * orig + 1] = fsum.y;
-            cf[3 * orig + 2] = fsum.z;
+            cf[3 * orig] = double(fw.x);
+            cf[3 * orig + 1] = double(fw.y);
+            cf[3 * orig + 2] = double(fw.z);
           }
         }
       }
@@ -526,7 +677,8 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       c.r(c.L.RF + 12 * b + 11) = t.z;
     }
     store_sv(c, c.L.A + 6 * b, cb);
-    store_sv(c, c.L.F + 6 * b, p);
+    if (contacts) store_svd(c, c.L.F + 6 * b, sv_d(p) + wc);  // bias forces of contact mechanisms: FP64
+    else store_sv(c, c.L.F + 6 * b, p);
     if (fl & BF_BRANCH) {
       store_abi(c, c.L.AI + ABI_D * b, ABI{});  // accumulator for children other than b+1
       store_sv(c, c.L.V + 6 * b, vb);
@@ -555,12 +707,18 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     const int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
     const int tb = TOPO_D * b;
     ABI IA = body_abi(c, tb);
-    SV<R> pA = load_sv(c, c.L.F + 6 * b);
-    if (fl & BF_BRANCH) abi_add(IA, load_abi(c, c.L.AI + ABI_D * b));
-    if (ctarget == b) {
-      abi_add(IA, carryI);
-      pA = pA + carryP;
+    SV<double> pAd;  // FP64 copy (contact mechanisms) for u
+    SV<R> pA;
+    if (contacts) {
+      pAd = load_svd(c, c.L.F + 6 * b);
+      if (ctarget == b) pAd = pAd + sv_d(carryP);
+      pA = sv_r<R>(pAd);
+    } else {
+      pA = load_sv(c, c.L.F + 6 * b);
+      if (ctarget == b) pA = pA + carryP;
     }
+    if (fl & BF_BRANCH) abi_add(IA, load_abi(c, c.L.AI + ABI_D * b));
+    if (ctarget == b) abi_add(IA, carryI);
     const SV<R> cb = load_sv(c, c.L.A + 6 * b);
     SV<R> pa;  // bias force handed to the parent
     const bool to_parent = parent != 0;
@@ -597,7 +755,12 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       const V axr{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
       double u = have_tau ? tau[vo] : 0.0;
       if (type == 2 && (w1 & BF_SPRING)) u += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
-      u -= double(type == 1 ? dot(axr, pA.w) : dot(axr, pA.v));
+      if (contacts) {
+        const VD axd{c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
+        u -= type == 1 ? dot(axd, pAd.w) : dot(axd, pAd.v);
+      } else {
+        u -= double(type == 1 ? dot(axr, pA.w) : dot(axr, pA.v));
+      }
       if (!(D > 0.0)) st |= 2;  // GPB_ST_CHOL_FAIL
       const double Dinv = 1.0 / D;
       const int du = c.L.DU + DU_D * vo;
@@ -638,11 +801,12 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       for (int k = 0; k < 21; ++k) c.d(du + k) = L[k];
 #pragma unroll
       for (int k = 0; k < 6; ++k) c.d(du + 21 + k) = dinv[k];
-      const R pv6[6] = {pA.w.x, pA.w.y, pA.w.z, pA.v.x, pA.v.y, pA.v.z};
+      const SV<double> pp = contacts ? pAd : sv_d(pA);
+      const double pv6[6] = {pp.w.x, pp.w.y, pp.w.z, pp.v.x, pp.v.y, pp.v.z};
       R pa6[6];
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
-        const double u = (have_tau ? tau[vo + k] : 0.0) - double(pv6[k]);
+        const double u = (have_tau ? tau[vo + k] : 0.0) - pv6[k];
         c.d(du + 27 + k) = u;
         pa6[k] = R(double(pv6[k]) + u);  // floating joint: I^a = 0, p^a = p^A + u
       }
@@ -665,7 +829,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
           co = Rr[3 * i1 + i1];
           si = Rr[3 * i2 + i1];
         }
-        const ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si);
+        const ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si, bw_taxis(w1));
         if (pb == b - 1) {
           carryI = Ip;
         } else {
@@ -685,7 +849,8 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         carryP = fp;
         ctarget = pb;
       } else {
-        store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
+        if (contacts) store_svd(c, c.L.F + 6 * pb, load_svd(c, c.L.F + 6 * pb) + sv_d(fp));
+        else store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
         ctarget = -1;
       }
     } else {

@@ -26,7 +26,55 @@ __global__ void fma_chains(T* out, int iters, T a, T b, int active_lanes) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// FP32 -> FP64 conversions, each result consumed by an integer xor (so no
+// round trip can be folded away), 8 independent chains per thread.
+__global__ void cvt_chains(long long* out, int iters) {
+  float f[8];
+  long long acc = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) f[j] = threadIdx.x * 1e-3f + j;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      f[j] = f[j] * 1.0001f + 1e-3f;
+      acc ^= __double_as_longlong((double)f[j]);
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
 }  // namespace
+
+// FP32 -> FP64 conversion throughput in G conversions/s (all lanes active).
+extern "C" int gpb_cvt_peak(int device, double* gops) {
+  if (!gops) return GPB_E_INVAL;
+  if (cudaSetDevice(device) != cudaSuccess) return GPB_E_CUDA;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  const int threads = 256, blocks = sms * 8, iters = 256;
+  void* out = nullptr;
+  if (cudaMalloc(&out, (size_t)blocks * threads * 8) != cudaSuccess) return GPB_E_NOMEM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(e0);
+    cvt_chains<<<blocks, threads>>>((long long*)out, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess) return GPB_E_CUDA;
+  *gops = 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e9;
+  return GPB_OK;
+}
 
 // TFLOP/s (2 per FMA, counted for active lanes only) of `precision`
 // (GPB_FP64 / GPB_MIXED = FP32) with `active_lanes` of every warp issuing.

@@ -138,6 +138,7 @@ SIGNATURES = [
                                    P_i32, P_i32, P_f64, P_i32, P_f64, P_i32, P_f64, P_f64, P_f64]),
     ("gpb_open_loop_tau", C.c_double, [C.c_uint32, C.c_int64, C.c_int64, C.c_int32, C.c_double]),
     ("gpb_fma_peak", C.c_int, [C.c_int, C.c_int, C.c_int, P_f64]),
+    ("gpb_cvt_peak", C.c_int, [C.c_int, P_f64]),
     ("gpb_dynamics_static", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                       C.c_void_p, C.c_void_p]),
     ("gpb_server_plan", C.c_int, [C.POINTER(GpbServerOpts), P_i32, P_i64]),

@@ -422,6 +422,10 @@ int gpb_server_stats_get(const gpb_server* server, gpb_server_stats* stats);
  * counting 2 flops per fused multiply-add of the `active_lanes` (1..32) lanes
  * of each warp that issue: the roofline denominator of the batched step. */
 int gpb_fma_peak(int device, int precision, int active_lanes, double* tflops);
+/* FP32 → FP64 conversion throughput (G conversions/s, all lanes active): on
+ * GB300 conversions share the FP64 unit's rate, which decides how a mixed form
+ * splits its work. */
+int gpb_cvt_peak(int device, double* gops);
 
 #ifdef __cplusplus
 }
