@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--instances", type=int, default=65536)
     ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--mix-chains", type=int, default=0,
+                    help="also step this many serial chains in the same batch (one control law for all)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--precision", default="all", choices=["all", "fp64", "mixed", "refined"])
     ap.add_argument("--serve", action="store_true",
@@ -258,6 +260,11 @@ def run_gpu(args):
     ctx = gpb.Context(local)
     # weak scaling: every rank owns its own instances (seed offset by rank)
     M, q0, v0, aux = Model.from_config(args.config, args.instances, seed=shard_seed(args.seed, rank))
+    if args.mix_chains > 0:  # e.g. quadrupeds and chains in the same persistent launch
+        M2, q2, v2, _ = Model.from_config(1, args.mix_chains, seed=shard_seed(args.seed, rank) + 7)
+        M = Model.concat([M, M2])
+        q0, v0 = np.concatenate([q0, q2]), np.concatenate([v0, v2])
+        aux = np.concatenate([aux, np.zeros_like(v2)])  # PD targets 0 for the chains
     B = Batch(M, ctx)
     kw = dict(control=CONTROL[args.config], tau=aux if args.config == 3 else None, seed=7,
               resample_every=10, sigma=1.0, kp=50.0, kd=2.0)
@@ -364,12 +371,35 @@ def run_gpu(args):
             "mixed": "FP64 share of the mixed articulated-body algorithm (gpb.flops.aba_model_flops(mixed=True))",
             "refined": "CRBA-equivalent flops (the FP64 residual is a part of them)"}
 
+    # DRAM bytes per instance-step from the committed ncu capture (small case of the
+    # same workload), scaled to this launch's completed instance-steps
+    try:
+        tb = json.loads((ROOT / "profiles" / "dram_traffic_per_instance_step.json").read_text())
+        traffic_per = tb.get(CONFIG_NAME[args.config], {})
+    except (OSError, ValueError):
+        traffic_per = {}
+    hbm_peak = None
+    try:
+        hbm_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        pass
+
     def roof(name, res):
         ach = res["flops"] / (res["kernel_ms"] * 1e-3) / 1e12
         per = res["flops"] / max(res["done"], 1.0)
-        return {"bound": "fp64", "achieved": ach, "peak": p64, "unit": "TFLOP/s", "frac": ach / p64,
-                "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (gpb_fma_peak), this run",
-                "work": f"{per:.0f} FP64 flops per completed instance-step (mean): {WORK[name]}"}
+        out = {"bound": "fp64", "achieved": ach, "peak": p64, "unit": "TFLOP/s", "frac": ach / p64,
+               "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (gpb_fma_peak), this run",
+               "work": f"{per:.0f} FP64 flops per completed instance-step (mean): {WORK[name]}"}
+        t = traffic_per.get(name)
+        if t and not args.mix_chains:
+            bytes_launch = t["dram_bytes_per_instance_step"] * res["done"]
+            out["traffic"] = bytes_launch
+            out["traffic_source"] = "ncu dram__bytes_read+write, " + t["capture"] + ", scaled to this launch"
+            if hbm_peak:
+                gbs = bytes_launch / (res["kernel_ms"] * 1e-3) / 1e9
+                out["hbm"] = {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+        return out
 
     DTYPE = {"fp64_crba": "f64", "fp64": "f64",
              "mixed": "f32 kinematics/bias + f64 articulated inertias + f64 state",
@@ -382,7 +412,8 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": DTYPE[head_name],
         "data": "synthetic (seeded Philox4x32-10 draws of the configuration's distributions)",
-        "config": {"workload": f"{CONFIG_NAME[args.config]} x {args.instances} per GPU",
+        "config": {"workload": f"{CONFIG_NAME[args.config]} x {args.instances}"
+                               + (f" + serial-chain x {args.mix_chains}" if args.mix_chains else "") + " per GPU",
                    "precision_mode": head_name, "algorithm": ALGO[head_name],
                    "dof": "U{2..48}" if args.config == 1 else None, "dt": dt,
                    "integrator": "semi-implicit Euler", "control": CONTROL[args.config],
@@ -405,7 +436,7 @@ def run_gpu(args):
     line["peaks_measured"] = {"fp64_tflops": p64, "fp32_tflops": p32}
     line["clocks"] = head["clocks"]
     line["failed_instances"] = {k: r["failed_instances"] for k, r in results.items()}
-    line["completed_fraction"] = {k: r["done"] / (args.instances * world * args.steps)
+    line["completed_fraction"] = {k: r["done"] / ((args.instances + args.mix_chains) * world * args.steps)
                                   for k, r in results.items()}
     line["e2e"] = {"value": e2e_done / e2e_s, "unit": UNIT,
                    "h2d_bytes_per_step": (qn.nbytes + vn.nbytes) / args.steps,
