@@ -754,13 +754,15 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       // u = τ + τ_spring − Sᵀ p^A
       const V axr{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
       double u = have_tau ? tau[vo] : 0.0;
-      if (type == 2 && (w1 & BF_SPRING)) u += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
+      if (type == 2 && (w1 & BF_SPRING) && c.springs)
+        u += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
       if (contacts) {
         const VD axd{c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
         u -= type == 1 ? dot(axd, pAd.w) : dot(axd, pAd.v);
       } else {
         u -= double(type == 1 ? dot(axr, pA.w) : dot(axr, pA.v));
       }
+      if (type == 1) D += c.td(tb + TD_ARMATURE);  // revolute armature (src/hybrid/articulated/mod.rs:244-247)
       if (!(D > 0.0)) st |= 2;  // GPB_ST_CHOL_FAIL
       const double Dinv = 1.0 / D;
       const int du = c.L.DU + DU_D * vo;
@@ -865,7 +867,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     const int tb = TOPO_D * b;
     SV<R> a;
     if (parent == 0) {
-      a = {zero, {R(0), R(0), R(GRAVITY)}};  // inverse gravity (src/dynamics.rs:211-218)
+      a = {zero, {R(0), R(0), R(c.grav)}};  // inverse gravity (src/dynamics.rs:211-218)
     } else if (parent == b) {
       a = ap_;
     } else {

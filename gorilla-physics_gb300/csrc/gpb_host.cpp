@@ -101,6 +101,9 @@ int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
   for (int b = 0; b < I.nb; ++b) {
     int t = m->joint_type[I.j0 + b], p = m->joint_parent[I.j0 + b];
     if (t < 0 || t > 3) return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": bad joint type");
+    if (m->joint_armature && m->joint_armature[I.j0 + b] != 0.0 && t != GPB_JOINT_REVOLUTE)
+      return fail(GPB_E_INVAL, "instance " + std::to_string(i) +
+                                   ": armature is only supported on revolute joints");  // src/joint/mod.rs:105-109
     if (p < 0 || p > b)
       return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": joint " + std::to_string(b + 1) +
                                    " has parent " + std::to_string(p) + " (must be < its own number)");
@@ -340,6 +343,13 @@ extern "C" int gpb_batch_set_algorithm(gpb_batch* b, int algorithm) {
   return GPB_OK;
 }
 
+extern "C" int gpb_batch_set_gravity(gpb_batch* b, double g) {
+  if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_gravity: batch is NULL");
+  if (!std::isfinite(g)) return fail(GPB_E_INVAL, "gpb_batch_set_gravity: g must be finite");
+  b->gravity = g;
+  return GPB_OK;
+}
+
 extern "C" int gpb_batch_set_coop(gpb_batch* b, int min_dof) {
   if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_coop: batch is NULL");
   if (min_dof < -1 || min_dof > GPB_MAX_DOF)
@@ -442,6 +452,33 @@ extern "C" int gpb_dynamics(gpb_batch* b, const double* tau, int precision, doub
   if (contact_force && b->nc_total)
     CUDA_TRY(cudaMemcpyAsync(contact_force, b->stage_c.p, 3 * b->nc_total * sizeof(double),
                              cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return GPB_OK;
+}
+
+extern "C" int gpb_free_velocity(gpb_batch* b, double dt, const double* tau, int precision, double* v_free) {
+  if (!b || !v_free) return fail(GPB_E_INVAL, "gpb_free_velocity: NULL argument");
+  if (int r = check_enums(0, precision)) return r;
+  if (!std::isfinite(dt)) return fail(GPB_E_INVAL, "gpb_free_velocity: dt must be finite");
+  CUDA_TRY(cudaSetDevice(b->ctx->device));
+  cudaStream_t s = b->ctx->stream;
+  StepParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.precision = precision;
+  p.tau_mode = tau ? 1 : 0;
+  p.free_velocity = 1;
+  p.vfree_dt = dt;
+  if (tau) {
+    int r = upload_user(b, tau, b->nv_total, b->stage_v, b->vmap, b->v_slots, b->tau_in);
+    if (r) return r;
+  }
+  p.qdd_out = b->stage_v.p;
+  DeviceBatch db = b->dev();
+  db.plain = 1;
+  CUDA_TRY(launch_dynamics(db, p, s));
+  b->ctx->launches++;
+  if (b->nv_total)
+    CUDA_TRY(cudaMemcpyAsync(v_free, b->stage_v.p, b->nv_total * sizeof(double), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   return GPB_OK;
 }

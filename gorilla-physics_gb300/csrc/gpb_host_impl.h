@@ -180,6 +180,7 @@ void fill_lane(const gpb_model* m, int64_t inst, const InstInfo& I, const PackDe
     for (int e = 0; e < 10; ++e) vals[TD_INERTIA + e] = in[e];
     vals[TD_SPRING] = sk;
     vals[TD_SPRING + 1] = sl;
+    vals[TD_ARMATURE] = m->joint_armature ? m->joint_armature[j] : 0.0;
     for (int e = 0; e < TOPO_D; ++e) S.td((P.topo * TOPO_D + TOPO_D * b + e) * L + l, vals[e]);
     // state maps and the zero state (identity pose for floating joints)
     for (int e = 0; e < joint_nq(t); ++e) S.qmap((P.q + qo + e) * L + l, q_user + qo + e);
@@ -210,6 +211,7 @@ struct gpb_batch {
   int warps_per_sm = 0;  // resident warps per SM of the step kernel (0 = occupancy limit)
   int coop_min_dof = -1; // block-cooperative packs: DOF threshold (-1 = default, 0 = off)
   int algorithm = GPB_ALGO_CRBA;
+  double gravity = 9.81;  // src/lib.rs:39
   std::vector<int64_t> q_off, v_off, c_off;  // user layout, [n+1]
   int64_t nq_total = 0, nv_total = 0, nc_total = 0;
   std::vector<gpb::PackDesc> packs_h;
@@ -250,6 +252,7 @@ struct gpb_batch {
     b.nc_total = nc_total;
     b.queue = queue.p;
     b.algorithm = algorithm;
+    b.gravity = gravity;
     return b;
   }
   void release() {

@@ -32,8 +32,8 @@ constexpr uint32_t BW_TAXIS = 1u << 24;
 __host__ __device__ inline int bw_taxis(uint32_t w1) { return (w1 & BW_TAXIS) ? (int)((w1 >> 25) & 3u) : -1; }
 
 // Doubles (and floats) of one body in the topology table.
-constexpr int TOPO_D = 27;  // Rinit (9, row-major), tinit (3), axis (3), inertia (10), spring (2)
-constexpr int TD_RINIT = 0, TD_TINIT = 9, TD_AXIS = 12, TD_INERTIA = 15, TD_SPRING = 25;
+constexpr int TOPO_D = 28;  // Rinit (9, row-major), tinit (3), axis (3), inertia (10), spring (2), armature
+constexpr int TD_RINIT = 0, TD_TINIT = 9, TD_AXIS = 12, TD_INERTIA = 15, TD_SPRING = 25, TD_ARMATURE = 27;
 constexpr int CTC_D = 6;    // location (3), k, radius, damping
 constexpr int HS_D = 8;     // point (3), normal (3), alpha, mu
 constexpr int LANE_I = 8;   // per-lane ints: instance, nb, nq, nv, nc, nh, contact model, pad
@@ -126,6 +126,8 @@ struct DeviceBatch {
   int64_t nq_total, nv_total, nc_total;
   int32_t* queue;          // persistent-kernel work counters: [0] per-warp packs, [1] block packs
   int32_t algorithm;       // GPB_ALGO_CRBA or GPB_ALGO_ABA
+  double gravity;          // m/s² along −z (9.81 unless set)
+  int32_t plain;           // 1: no contact points, no prismatic springs (free_velocity)
   // serving pool only (all null for a batch)
   LaneJob* jobs;           // per-slot jobs
   const int32_t* active;   // packs to run in this launch (nactive of them)
@@ -163,6 +165,8 @@ struct StepParams {
   double* cforce_out;   // dynamics-only: user-order contact forces (device)
   int32_t tau_mode;     // dynamics/step: 0 = zero torque, 1 = tau_in holds torques
   int32_t ncoop;        // packs [0, ncoop) are stepped by a whole 4-warp block
+  int32_t free_velocity;  // dynamics-only: write v + vfree_dt·q̈ (no contacts, no springs)
+  double vfree_dt;
 };
 
 // Launchers (gpb_kernels.cu).  All return a cudaError_t.

@@ -28,7 +28,6 @@
 
 namespace gpb {
 
-constexpr double GRAVITY = 9.81;  // src/lib.rs:39
 
 __host__ __device__ double open_loop_tau(uint32_t seed, int64_t inst, int64_t block, int32_t dof,
                                          double sigma) {
@@ -67,6 +66,8 @@ struct RealTopo<float> {
 template <typename R>
 struct LaneCtx {
   int lane, nb, nq, nv, nc, nh, model, chain;
+  int springs;  // prismatic springs act (off for Articulated::free_velocity)
+  double grav;  // gravitational acceleration along −z
   const uint32_t* W;  // topology words (row base applied, lane applied)
   const R* T;         // topology reals
   const int32_t* CI;  // contact ints
@@ -79,11 +80,14 @@ struct LaneCtx {
   R* sR;              // scratch viewed as R (row pitch = LANES * 8 bytes)
   double* sD;         // scratch viewed as double
   char* s0;           // scratch row 0, lane 0
-  __device__ __forceinline__ uint32_t w(int e) const { return W[(size_t)e * LANES]; }
-  __device__ __forceinline__ R t(int e) const { return T[(size_t)e * LANES]; }
-  __device__ __forceinline__ double td(int e) const { return TDD[(size_t)e * LANES]; }
-  __device__ __forceinline__ double cdd(int e) const { return CDD[(size_t)e * LANES]; }
-  __device__ __forceinline__ double hdd(int e) const { return HDD[(size_t)e * LANES]; }
+  // the mechanism tables are read-only for the whole launch: read them through
+  // the non-coherent path, so the loads may be issued early and need no
+  // ordering against the scratch stores
+  __device__ __forceinline__ uint32_t w(int e) const { return __ldg(W + (size_t)e * LANES); }
+  __device__ __forceinline__ R t(int e) const { return __ldg(T + (size_t)e * LANES); }
+  __device__ __forceinline__ double td(int e) const { return __ldg(TDD + (size_t)e * LANES); }
+  __device__ __forceinline__ double cdd(int e) const { return __ldg(CDD + (size_t)e * LANES); }
+  __device__ __forceinline__ double hdd(int e) const { return __ldg(HDD + (size_t)e * LANES); }
   // R-typed scratch element (e in rows of 8-byte words)
   __device__ __forceinline__ R& r(int e) const {
     return *reinterpret_cast<R*>(reinterpret_cast<char*>(sR) + (size_t)e * LANES * 8);
@@ -412,7 +416,7 @@ template <typename R, typename RC>
 __device__ __noinline__ void lane_sweeps(const LaneCtx<R>& cin, Col<double> q, Col<double> v, Col<double> tau,
                                          bool have_tau, Col<double> cforce, bool want_cf) {
   const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
-  const R g = R(GRAVITY);
+  const R g = R(c.grav);
   // ---- outward sweep --------------------------------------------------
   M3<R> Rp;
   V3<R> pp;
@@ -606,7 +610,7 @@ __device__ __noinline__ void lane_sweeps(const LaneCtx<R>& cin, Col<double> q, C
     for (int k = 0; k < nvb; ++k) {
       SV<R> Sk = load_sv(c, c.L.S + 6 * (vo + k));
       double rhs = have_tau ? tau[vo + k] : 0.0;
-      if (type == 2 && (w1 & BF_SPRING)) {  // src/dynamics.rs:298-315
+      if (type == 2 && (w1 & BF_SPRING) && c.springs) {  // src/dynamics.rs:298-315
         const int tb = TOPO_D * b;
         double ks = double(c.t(tb + TD_SPRING)), ls = double(c.t(tb + TD_SPRING + 1));
         rhs += -ks * (q[qo] - ls);
@@ -654,6 +658,8 @@ __device__ __noinline__ void lane_fill(const LaneCtx<R>& cin, int w, int nw) {
     const int nvb = type == 3 ? 6 : (type == 0 ? 0 : 1);
     if (nvb == 0) continue;
     const SI<R> Ic = load_si(c, c.L.I + 10 * b);
+    // a revolute joint's armature adds to its diagonal (src/hybrid/articulated/mod.rs:244-247)
+    const R arm = type == 1 ? c.t(TOPO_D * b + TD_ARMATURE) : R(0);
     for (int k = 0; k < nvb; ++k) {
       const int row = vo + k;
       if ((row >> 2) % nw != w) continue;
@@ -661,7 +667,8 @@ __device__ __noinline__ void lane_fill(const LaneCtx<R>& cin, int w, int nw) {
       const SV<R> Fk = imul(Ic, Sk);
       for (int l = 0; l <= k; ++l) {
         const SV<R> Sl = l == k ? Sk : load_sv(c, c.L.S + 6 * (vo + l));
-        c.template x<RC>(c.L.M + tix(row, vo + l)) = RC(sdot2(Fk, Sl));
+        const R h = sdot2(Fk, Sl);
+        c.template x<RC>(c.L.M + tix(row, vo + l)) = RC(l == k ? h + arm : h);
       }
       int a = parent;
       while (a != 0) {
@@ -875,10 +882,12 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   c.nb = li[1 * LANES];
   c.nq = li[2 * LANES];
   c.nv = li[3 * LANES];
-  c.nc = li[4 * LANES];
+  c.nc = b.plain ? 0 : li[4 * LANES];  // free_velocity: no contact points
   c.nh = li[5 * LANES];
   c.model = li[6 * LANES];
   c.chain = pd.chain;
+  c.springs = b.plain ? 0 : 1;
+  c.grav = b.gravity;
   c.W = b.topoW + pd.topo * 2 * LANES + lane;
   c.T = RealTopo<R>::topo(b) + pd.topo * TOPO_D * LANES + lane;
   c.CI = b.ctcI + pd.ctc * LANES + lane;
@@ -1049,7 +1058,11 @@ __global__ void __launch_bounds__(128) dynamics_kernel(DeviceBatch b, StepParams
   const int st = ev(q, v, tin, p.tau_mode != 0, qdd, cf, true);
   b.status[(int64_t)pk * LANES + lane] |= st;
   const int64_t* vm = b.vmap + pd.v * LANES + lane;
-  for (int i = 0; i < c.nv; ++i) p.qdd_out[vm[(size_t)i * LANES]] = qdd[i];
+  if (p.free_velocity) {  // Articulated::free_velocity: v + dt·q̈
+    for (int i = 0; i < c.nv; ++i) p.qdd_out[vm[(size_t)i * LANES]] = v[i] + qdd[i] * p.vfree_dt;
+  } else {
+    for (int i = 0; i < c.nv; ++i) p.qdd_out[vm[(size_t)i * LANES]] = qdd[i];
+  }
   if (p.cforce_out) {
     const int64_t* cm = b.cmap + pd.ctc * 3 * LANES + lane;
     for (int k = 0; k < 3 * c.nc; ++k) p.cforce_out[cm[(size_t)k * LANES]] = cf[k];

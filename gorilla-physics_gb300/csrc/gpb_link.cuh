@@ -76,7 +76,7 @@ __device__ __noinline__ int lane_link(const LaneCtx<R>& cin, Col<double> q, Col<
       om = zero;
       vl = zero;
       al = zero;
-      ac = {R(0), R(0), R(GRAVITY)};  // inverse gravity (src/dynamics.rs:211-218)
+      ac = {R(0), R(0), R(c.grav)};  // inverse gravity (src/dynamics.rs:211-218)
     } else if (parent == b) {
       om = pw_;
       vl = pv_;
@@ -271,11 +271,12 @@ __device__ __noinline__ int lane_link(const LaneCtx<R>& cin, Col<double> q, Col<
     if (type == 1 || type == 2) ax = {c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
     for (int k = 0; k < nvb; ++k) {
       double r = have_tau ? tau[vo + k] : 0.0;
-      if (type == 2 && (w1 & BF_SPRING)) {  // src/dynamics.rs:298-315
+      if (type == 2 && (w1 & BF_SPRING) && c.springs) {  // src/dynamics.rs:298-315
         r += -double(c.t(tb + TD_SPRING)) * (q[qo] - double(c.t(tb + TD_SPRING + 1)));
       }
+      const double arm = type == 1 ? double(c.t(tb + TD_ARMATURE)) : 0.0;  // revolute armature
       if (RESIDUAL) {  // difference of nearly equal terms: form it in FP64
-        c.template x<RC>(c.L.rhs + vo + k) = RC(r - double(s_dot<R>(type, ax, k, f)));
+        c.template x<RC>(c.L.rhs + vo + k) = RC(r - double(s_dot<R>(type, ax, k, f)) - arm * xacc[vo + k]);
         continue;
       }
       c.template x<RC>(c.L.rhs + vo + k) = RC(RC(r) - RC(s_dot<R>(type, ax, k, f)));
@@ -290,7 +291,10 @@ __device__ __noinline__ int lane_link(const LaneCtx<R>& cin, Col<double> q, Col<
         else Sk.v = {e[0], e[1], e[2]};
       }
       SV<R> F = imul(Ic, Sk);
-      for (int l = 0; l <= k; ++l) c.template x<RC>(c.L.M + tix(row, vo + l)) = RC(s_dot<R>(type, ax, l, F));
+      for (int l = 0; l <= k; ++l) {
+        const R h = s_dot<R>(type, ax, l, F);
+        c.template x<RC>(c.L.M + tix(row, vo + l)) = RC(l == k ? h + R(arm) : h);
+      }
       int ch = b, a = parent;
       while (a != 0) {
         M3<R> Rr;

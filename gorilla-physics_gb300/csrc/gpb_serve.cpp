@@ -55,7 +55,8 @@ struct ClassInfo {
 struct OwnedModel {
   std::vector<int32_t> joint_offset{0, 0}, joint_type, joint_parent, contact_offset{0, 0}, contact_body,
       halfspace_offset{0, 0}, contact_model;
-  std::vector<double> joint_iso, joint_axis, joint_spring, body_inertia, contact_params, halfspace_params;
+  std::vector<double> joint_iso, joint_axis, joint_spring, body_inertia, contact_params, halfspace_params,
+      joint_armature;
   gpb_model view() const {
     gpb_model m;
     std::memset(&m, 0, sizeof(m));
@@ -73,6 +74,7 @@ struct OwnedModel {
     m.halfspace_offset = halfspace_offset.data();
     m.halfspace_params = halfspace_params.data();
     m.contact_model = contact_model.data();
+    m.joint_armature = joint_armature.data();
     return m;
   }
 };
@@ -407,6 +409,10 @@ extern "C" int gpb_server_submit(gpb_server* S, const gpb_model* m, int64_t firs
     else
       O.joint_spring.assign(2 * (size_t)I.nb, 0.0);
     O.body_inertia.assign(m->body_inertia + 10 * (size_t)I.j0, m->body_inertia + 10 * (size_t)(I.j0 + I.nb));
+    if (m->joint_armature)
+      O.joint_armature.assign(m->joint_armature + I.j0, m->joint_armature + I.j0 + I.nb);
+    else
+      O.joint_armature.assign((size_t)I.nb, 0.0);
     O.contact_offset = {0, I.nc};
     if (I.nc) {
       O.contact_body.assign(m->contact_body + I.c0, m->contact_body + I.c0 + I.nc);

@@ -45,6 +45,7 @@ class GpbModel(C.Structure):
         ("halfspace_offset", P_i32),
         ("halfspace_params", P_f64),
         ("contact_model", P_i32),
+        ("joint_armature", P_f64),
     ]
 
 
@@ -128,6 +129,8 @@ SIGNATURES = [
     ("gpb_batch_set_launch", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_batch_set_coop", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_batch_set_algorithm", C.c_int, [C.c_void_p, C.c_int]),
+    ("gpb_batch_set_gravity", C.c_int, [C.c_void_p, C.c_double]),
+    ("gpb_free_velocity", C.c_int, [C.c_void_p, C.c_double, P_f64, C.c_int, P_f64]),
     ("gpb_batch_autotune", C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_int, C.POINTER(GpbControl), C.c_int,
                                      P_i32, P_i32]),
     ("gpb_launch_count", C.c_int64, [C.c_void_p]),

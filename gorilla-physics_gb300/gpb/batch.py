@@ -155,6 +155,17 @@ class Batch:
         _abi.check(_abi.lib().gpb_batch_set_mapping(self.h, lanes_per_instance),
                    "gpb_batch_set_mapping")
 
+    def set_gravity(self, g: float) -> None:
+        """Gravitational acceleration along −z (default 9.81; 0 = off)."""
+        _abi.check(_abi.lib().gpb_batch_set_gravity(self.h, g), "gpb_batch_set_gravity")
+
+    def free_velocity(self, dt: float, tau=None, precision: int = _abi.FP64) -> np.ndarray:
+        """Articulated::free_velocity (src/hybrid/articulated/mod.rs:124-199): v + dt·M⁻¹(τ − c)."""
+        t = None if tau is None else np.ascontiguousarray(tau, dtype=np.float64).ravel()
+        out = np.zeros(max(self.nv, 1))
+        _abi.check(_abi.lib().gpb_free_velocity(self.h, dt, _p(t), precision, _p(out)), "gpb_free_velocity")
+        return out[:self.nv]
+
     def set_algorithm(self, algorithm: int) -> None:
         """ALGO_CRBA (the reference's route, default) or ALGO_ABA (articulated-body algorithm)."""
         _abi.check(_abi.lib().gpb_batch_set_algorithm(self.h, algorithm), "gpb_batch_set_algorithm")

@@ -95,6 +95,14 @@ class _Joint:
     axis: tuple = (0.0, 0.0, 1.0)
     spring: tuple | None = None  # (k, rest length), prismatic only
     kind: int = _abi.FIXED
+    armature: float = 0.0        # reflected rotor inertia, revolute only
+
+    def with_armature(self, armature: float) -> "_Joint":
+        """Joint::with_armature (src/joint/mod.rs:105-109)."""
+        if self.kind != _abi.REVOLUTE:
+            raise AssertionError("armature is only supported on revolute joints")
+        self.armature = float(armature)
+        return self
 
 
 def RevoluteJoint(transform: Transform3D, axis) -> _Joint:
@@ -184,11 +192,13 @@ class Model:
 
     FIELDS = ("joint_offset", "joint_type", "joint_parent", "joint_iso", "joint_axis",
               "joint_spring", "body_inertia", "contact_offset", "contact_body", "contact_params",
-              "halfspace_offset", "halfspace_params", "contact_model")
+              "halfspace_offset", "halfspace_params", "contact_model", "joint_armature")
 
     def __init__(self, **arrays):
         i32 = ("joint_offset", "joint_type", "joint_parent", "contact_offset", "contact_body",
                "halfspace_offset", "contact_model")
+        if arrays.get("joint_armature") is None:  # optional: no armature
+            arrays["joint_armature"] = np.zeros(len(np.asarray(arrays["joint_type"]).ravel()))
         for name in self.FIELDS:
             a = arrays[name]
             dt = np.int32 if name in i32 else np.float64
@@ -199,7 +209,7 @@ class Model:
     # -- construction -----------------------------------------------------
     @classmethod
     def from_mechanisms(cls, mechs: Sequence[MechanismState]) -> "Model":
-        jo, jt, jp, iso, ax, sp, inert = [0], [], [], [], [], [], []
+        jo, jt, jp, iso, ax, sp, inert, arm = [0], [], [], [], [], [], [], []
         co, cb, cp, ho, hp, cm = [0], [], [], [0], [], []
         for m in mechs:
             for j, b, p in zip(m.treejoints, m.bodies, m.parents):
@@ -208,6 +218,7 @@ class Model:
                 iso.extend(list(j.transform.rotation) + list(j.transform.translation))
                 ax.extend(j.axis)
                 sp.extend(j.spring if j.spring is not None else (0.0, 0.0))
+                arm.append(j.armature)
                 I = b.inertia
                 M = np.asarray(I.moment, float)
                 inert.extend([I.mass, *np.asarray(I.cross_part, float),
@@ -224,7 +235,8 @@ class Model:
             cm.append(m.contact_model)
         return cls(joint_offset=jo, joint_type=jt, joint_parent=jp, joint_iso=iso, joint_axis=ax,
                    joint_spring=sp, body_inertia=inert, contact_offset=co, contact_body=cb,
-                   contact_params=cp, halfspace_offset=ho, halfspace_params=hp, contact_model=cm)
+                   contact_params=cp, halfspace_offset=ho, halfspace_params=hp, contact_model=cm,
+                   joint_armature=arm)
 
     @classmethod
     def from_config(cls, config: int, n: int, seed: int = 0,
@@ -296,6 +308,7 @@ class Model:
             parts["joint_iso"].append(self.joint_iso[7 * j0:7 * j1])
             parts["joint_axis"].append(self.joint_axis[3 * j0:3 * j1])
             parts["joint_spring"].append(self.joint_spring[2 * j0:2 * j1])
+            parts["joint_armature"].append(self.joint_armature[j0:j1])
             parts["body_inertia"].append(self.body_inertia[10 * j0:10 * j1])
             parts["contact_body"].append(self.contact_body[c0:c1])
             parts["contact_params"].append(self.contact_params[6 * c0:6 * c1])
@@ -314,7 +327,7 @@ class Model:
         out = {}
         for name in ("joint_type", "joint_parent", "joint_iso", "joint_axis", "joint_spring",
                      "body_inertia", "contact_body", "contact_params", "halfspace_params",
-                     "contact_model"):
+                     "contact_model", "joint_armature"):
             out[name] = np.concatenate([getattr(m, name)[:cls._used(m, name)] for m in models])
         for name in ("joint_offset", "contact_offset", "halfspace_offset"):
             parts, base = [np.zeros(1, np.int64)], 0
@@ -330,7 +343,7 @@ class Model:
         """Length of the used part of a table (struct() may pad empty tables to one entry)."""
         nj, nc, nh = int(m.joint_offset[-1]), int(m.contact_offset[-1]), int(m.halfspace_offset[-1])
         per = {"joint_type": nj, "joint_parent": nj, "joint_iso": 7 * nj, "joint_axis": 3 * nj,
-               "joint_spring": 2 * nj, "body_inertia": 10 * nj, "contact_body": nc,
+               "joint_spring": 2 * nj, "joint_armature": nj, "body_inertia": 10 * nj, "contact_body": nc,
                "contact_params": 6 * nc, "halfspace_params": 8 * nh, "contact_model": m.n}
         return per[name]
 

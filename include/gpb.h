@@ -131,6 +131,11 @@ enum gpb_control {
  * halfspace_params[8h..] point (3), outward unit normal (3), alpha, mu
  *                   (src/collision/halfspace.rs:6-11)
  * contact_model[i]  gpb_contact_model of instance i
+ * joint_armature[j] reflected rotor inertia of a revolute joint, added to its
+ *                   diagonal of the mass matrix (src/joint/revolute.rs:29,
+ *                   src/hybrid/articulated/mod.rs:244-247); NULL = none.  The
+ *                   reference's continuous path has no such term, so leave it
+ *                   NULL for parity with dynamics_continuous.
  */
 typedef struct gpb_model {
   int64_t n_instances;
@@ -147,6 +152,7 @@ typedef struct gpb_model {
   const int32_t* halfspace_offset; /* [n_instances + 1] */
   const double* halfspace_params;
   const int32_t* contact_model;    /* [n_instances] */
+  const double* joint_armature;    /* [n_joints] or NULL */
 } gpb_model;
 
 /* Limits of one instance. */
@@ -291,6 +297,20 @@ int gpb_batch_set_coop(gpb_batch* batch, int min_dof);
 
 /* GPB_ALGO_CRBA (default) or GPB_ALGO_ABA for every later dynamics call. */
 int gpb_batch_set_algorithm(gpb_batch* batch, int algorithm);
+
+/* Gravitational acceleration along −z for every later call (default 9.81,
+ * src/lib.rs:39; 0 switches gravity off as Articulated::free_velocity's
+ * gravity_enabled = false does). */
+int gpb_batch_set_gravity(gpb_batch* batch, double g);
+
+/*
+ * Articulated::free_velocity (src/hybrid/articulated/mod.rs:124-199) for every
+ * instance: v + dt · M⁻¹ (τ − c(q, v)) with the armature on the mass matrix's
+ * diagonal and the batch's gravity; no contact points and no prismatic springs
+ * (the hybrid engine handles contact itself).  tau: nv_total doubles or NULL;
+ * v_free: nv_total doubles in the user order.
+ */
+int gpb_free_velocity(gpb_batch* batch, double dt, const double* tau, int precision, double* v_free);
 
 /* Autotuner: times `trial_steps` steps of this batch (its own mechanisms,
  * state, step size, integrator, precision and control law) for each launch

@@ -51,6 +51,7 @@ def lib():
         L.oracle_dims.argtypes = [vp, C.c_int64, P_i32, P_i32, P_i32]
         L.oracle_dynamics.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_int, P_f64, P_f64]
         L.oracle_mass_matrix.argtypes = [vp, C.c_int64, P_f64, P_f64]
+        L.oracle_free_velocity.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_double, C.c_int, P_f64]
         L.oracle_energy.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, P_f64]
         L.oracle_step.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_double, C.c_int, C.c_int]
         L.oracle_open_loop_tau.argtypes = [C.c_uint32, C.c_int64, C.c_int64, C.c_int32, C.c_double]
@@ -102,6 +103,14 @@ def dynamics(model, i, q, v, tau=None, solver=LU, contact_forces=False):
     if contact_forces:
         return qdd[:nv], st, cf[:3 * nc]
     return qdd[:nv], st
+
+
+def free_velocity(model, i, q, v, tau=None, dt=1e-3, gravity=True):
+    """Articulated::free_velocity of instance i (src/hybrid/articulated/mod.rs:124-199)."""
+    _, _, _, q, v, tau = _checked(model, i, q, v, tau)
+    out = np.zeros(max(v.size, 1))
+    st = lib().oracle_free_velocity(_m(model), i, _p(q), _p(v), _p(tau), dt, int(bool(gravity)), _p(out))
+    return out[:v.size], st
 
 
 def mass_matrix(model, i, q):

@@ -225,6 +225,7 @@ struct Joint {
   Iso init_iso;
   V3 axis;
   double spring_k, spring_l;
+  double armature;  // reflected rotor inertia (revolute), src/joint/revolute.rs:29
   int nq, nv, qo, vo;
 };
 struct Mechanism {
@@ -259,6 +260,7 @@ static bool load_mechanism(const gpb_model* m, int64_t inst, Mechanism& out) {
     J.axis = {ax[0], ax[1], ax[2]};
     J.spring_k = m->joint_spring ? m->joint_spring[2 * (size_t)j] : 0.0;
     J.spring_l = m->joint_spring ? m->joint_spring[2 * (size_t)j + 1] : 0.0;
+    J.armature = m->joint_armature ? m->joint_armature[j] : 0.0;
     switch (J.type) {
       case GPB_JOINT_FIXED: J.nq = 0; J.nv = 0; break;
       case GPB_JOINT_REVOLUTE:
@@ -536,7 +538,7 @@ static void contact_dynamics(const Mechanism& M, const std::vector<Iso>& X,
 // compute_torques (src/spatial/wrench.rs:96-126).
 static void dynamics_bias(const Mechanism& M, const std::vector<Iso>& X, const std::vector<SV>& jt,
                           const std::vector<SV>& T, const std::vector<SV>& Wc,
-                          std::vector<double>& c) {
+                          std::vector<double>& c, double gravity = GRAVITY) {
   int n = (int)M.joints.size();
   std::vector<SV> cor(n + 1, SV{{0, 0, 0}, {0, 0, 0}});
   for (int a = 0; a < n; ++a) {
@@ -549,7 +551,7 @@ static void dynamics_bias(const Mechanism& M, const std::vector<Iso>& X, const s
   }
   std::vector<SV> wr(n + 1, SV{{0, 0, 0}, {0, 0, 0}});
   for (int a = 0; a < n; ++a) {
-    SV acc{V3{0, 0, 0} + cor[a + 1].ang, V3{0, 0, GRAVITY} + cor[a + 1].lin};
+    SV acc{V3{0, 0, 0} + cor[a + 1].ang, V3{0, 0, gravity} + cor[a + 1].lin};
     Inertia I = inertia_transform(M.bodies[a], X[a + 1]);
     const SV& tw = T[a + 1];
     SV f = mul_inertia(I, acc.ang, acc.lin);
@@ -887,6 +889,36 @@ int oracle_dynamics(const gpb_model* m, int64_t inst, const double* q, const dou
   if (!orc::load_mechanism(m, inst, M)) return GPB_E_INVAL;
   orc::Work w;
   return orc::dynamics(M, q, v, tau, solver, qdd, contact_force, w);
+}
+
+// Articulated::free_velocity (src/hybrid/articulated/mod.rs:124-199,
+// update_mass_matrix 201-262): v + dt · M⁻¹ (τ − c) with the revolute
+// armature on M's diagonal (244-247), gravity switchable, no contacts and no
+// springs, solved by Cholesky as the reference does (mass_matrix.cholesky()).
+int oracle_free_velocity(const gpb_model* m, int64_t inst, const double* q, const double* v,
+                         const double* tau, double dt, int gravity_enabled, double* v_free) {
+  orc::Mechanism M;
+  if (!orc::load_mechanism(m, inst, M)) return GPB_E_INVAL;
+  orc::Work w;
+  const int n = (int)M.joints.size();
+  orc::bodies_to_root(M, q, w.X);
+  w.jt.resize(n);
+  for (int a = 0; a < n; ++a) w.jt[a] = orc::joint_twist(M.joints[a], v);
+  w.T.assign(n + 1, orc::SV{{0, 0, 0}, {0, 0, 0}});
+  for (int a = 0; a < n; ++a)
+    w.T[a + 1] = orc::sv_add(w.T[M.joints[a].parent], orc::twist_transform(w.jt[a], w.X[a + 1]));
+  orc::mass_matrix(M, w.X, w.M);
+  for (int a = 0; a < n; ++a) {
+    const orc::Joint& J = M.joints[a];
+    if (J.nv > 0) w.M[(size_t)J.vo * M.nv + J.vo] += J.armature;
+  }
+  w.Wc.assign(n + 1, orc::SV{{0, 0, 0}, {0, 0, 0}});
+  orc::dynamics_bias(M, w.X, w.jt, w.T, w.Wc, w.c, gravity_enabled ? orc::GRAVITY : 0.0);
+  std::vector<double> rhs(M.nv);
+  for (int i = 0; i < M.nv; ++i) rhs[i] = (tau ? tau[i] : 0.0) - w.c[i];
+  bool ok = M.nv == 0 || orc::chol_solve(w.M, M.nv, rhs);
+  for (int i = 0; i < M.nv; ++i) v_free[i] = v[i] + rhs[i] * dt;
+  return ok ? 0 : GPB_ST_CHOL_FAIL;
 }
 
 int oracle_mass_matrix(const gpb_model* m, int64_t inst, const double* q, double* H) {
