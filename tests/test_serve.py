@@ -65,8 +65,9 @@ def submit_all(S, M, q0, v0, aux, cfg, horizons, idx):
     return ids
 
 
-def run_server(ctx, M, q0, v0, aux, cfg, horizons, idx, precision, chunk=37, classes=CLASSES):
-    S = Server(ctx, classes, precision=precision, chunk_steps=chunk)
+def run_server(ctx, M, q0, v0, aux, cfg, horizons, idx, precision, chunk=37, classes=CLASSES,
+               algorithm=gpb.ALGO_CRBA):
+    S = Server(ctx, classes, precision=precision, chunk_steps=chunk, algorithm=algorithm)
     ids = submit_all(S, M, q0, v0, aux, cfg, horizons, idx)
     S.drain(100000)
     out = {i: S.result(r) for i, r in ids.items()}
@@ -75,16 +76,18 @@ def run_server(ctx, M, q0, v0, aux, cfg, horizons, idx, precision, chunk=37, cla
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", [gpb.FP64, gpb.MIXED, gpb.MIXED_REFINED])
-def test_alone_equals_mix_bit_for_bit(ctx, precision):
+@pytest.mark.parametrize("precision,algorithm", [(gpb.FP64, gpb.ALGO_CRBA), (gpb.MIXED, gpb.ALGO_CRBA),
+                                                 (gpb.MIXED_REFINED, gpb.ALGO_CRBA), (gpb.FP64, gpb.ALGO_ABA),
+                                                 (gpb.MIXED, gpb.ALGO_ABA)])
+def test_alone_equals_mix_bit_for_bit(ctx, precision, algorithm):
     M, q0, v0, aux, cfg = mix_model()
     rng = np.random.default_rng(5)
     horizons = rng.integers(40, 300, size=M.n)
-    mix = run_server(ctx, M, q0, v0, aux, cfg, horizons, range(M.n), precision)
+    mix = run_server(ctx, M, q0, v0, aux, cfg, horizons, range(M.n), precision, algorithm=algorithm)
     # one pack (32 slots) per class: the 40 acrobots and 40 chains queue, and
     # later requests run in slots freed by others (of other sizes for the chains)
     for i in (0, 35, 42, 77, 82, 86, 88):
-        alone = run_server(ctx, M, q0, v0, aux, cfg, horizons, [i], precision, chunk=53)[i]
+        alone = run_server(ctx, M, q0, v0, aux, cfg, horizons, [i], precision, chunk=53, algorithm=algorithm)[i]
         qa, va, sa, da, _ = alone
         qm, vm, sm, dm, _ = mix[i]
         assert sa == sm and da == dm == horizons[i]
