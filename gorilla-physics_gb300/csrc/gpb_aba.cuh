@@ -164,70 +164,6 @@ __device__ __forceinline__ void sym_pack(const double* F, double* S) {
   S[0] = F[0], S[1] = F[4], S[2] = F[8], S[3] = F[1], S[4] = F[2], S[5] = F[5];
 }
 
-// Rotation about principal axis K (compile-time indices) by (co, si) of the
-// three blocks, into full 3×3 arrays.
-template <int K>
-__device__ __forceinline__ void rotate_planar(const ABI& I, double co, double si, double* A, double* B, double* Cm) {
-  constexpr int i1 = (K + 1) % 3, i2 = (K + 2) % 3;
-  double a6[6], c6[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    a6[k] = I.A[k];
-    c6[k] = I.C[k];
-  }
-  sym_planar(a6, K, co, si);
-  sym_planar(c6, K, co, si);
-  sym_expand(a6, A);
-  sym_expand(c6, Cm);
-#pragma unroll
-  for (int k = 0; k < 9; ++k) B[k] = I.B[k];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {  // rows
-    const double x = B[3 * i1 + j], y = B[3 * i2 + j];
-    B[3 * i1 + j] = co * x - si * y;
-    B[3 * i2 + j] = si * x + co * y;
-  }
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {  // columns
-    const double x = B[3 * r + i1], y = B[3 * r + i2];
-    B[3 * r + i1] = co * x - si * y;
-    B[3 * r + i2] = si * x + co * y;
-  }
-}
-
-// The shift by t = τ e_J (compile-time J): with T = τ [e_J]× only the rows /
-// columns J+1, J+2 take part —
-//   W = T C': W[j1] = −τ C'[j2], W[j2] = τ C'[j1];  B'T: column j2 = −τ B'[:, j1],
-//   column j1 = τ B'[:, j2];  T C' T: (j1,j1) = −τ² C'_j2j2, (j2,j2) = −τ² C'_j1j1,
-//   (j1,j2) = τ² C'_j1j2.
-template <int J>
-__device__ __forceinline__ void shift_axis(const double* A, const double* B, const double* Cm, double tau, ABI& o) {
-  constexpr int j1 = (J + 1) % 3, j2 = (J + 2) % 3;
-  double W[9], BT[9], TCT[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) W[k] = BT[k] = TCT[k] = 0.0;
-#pragma unroll
-  for (int m = 0; m < 3; ++m) {
-    W[3 * j1 + m] = -tau * Cm[3 * j2 + m];
-    W[3 * j2 + m] = tau * Cm[3 * j1 + m];
-    BT[3 * m + j2] = -tau * B[3 * m + j1];
-    BT[3 * m + j1] = tau * B[3 * m + j2];
-  }
-  const double t2 = tau * tau;
-  TCT[3 * j1 + j1] = -t2 * Cm[3 * j2 + j2];
-  TCT[3 * j2 + j2] = -t2 * Cm[3 * j1 + j1];
-  TCT[3 * j1 + j2] = TCT[3 * j2 + j1] = t2 * Cm[3 * j1 + j2];
-  const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
-#pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    const int i = ii[k], j = jj[k];
-    o.A[k] = A[3 * i + j] - BT[3 * i + j] - BT[3 * j + i] - TCT[3 * i + j];
-    o.C[k] = Cm[3 * i + j];
-  }
-#pragma unroll
-  for (int k = 0; k < 9; ++k) o.B[k] = B[k] + W[k];
-}
-
 // General shift by t (T = [t]×): C_p = C', B_p = B' + T C',
 // A_p = A' − B'T − (B'T)ᵀ − T C' T.
 __device__ __forceinline__ void shift_general(const double* A, const double* B, const double* Cm, V3<double> t,
@@ -261,52 +197,28 @@ __device__ __forceinline__ void shift_general(const double* A, const double* B, 
 
 // Articulated inertia of a child, in the child frame, expressed in the parent
 // frame: X*ᵀ I X for the child→parent transform (rotation Rr, child origin t):
-// every block rotated (R S Rᵀ), then shifted by t.  `planar` ≥ 0: Rr is the
-// rotation about that principal axis by (co, si); `taxis` ≥ 0: t lies along
-// that axis (3: t = 0).  When every active lane of the warp has the same
-// (planar, taxis) — mechanisms of one design — code with compile-time indices
-// runs; otherwise (lanes with different axes) one runtime-indexed path serves
-// all lanes without divergence.
+// every block rotated (R S Rᵀ) — a planar rotation when `planar` ≥ 0 (the
+// rotation about that principal axis by (co, si)) — then shifted by t.  One
+// code path for every lane, so a mechanism's result does not depend on the
+// mechanisms sharing its warp (lanes with different axes run it together).
 __device__ __forceinline__ ABI abi_to_parent(const ABI& I, const double* Rr, V3<double> t, int planar, double co,
-                                             double si, int taxis) {
-  const unsigned am = __activemask();
-  const int key = (planar + 1) * 8 + (taxis + 1);
-  const bool uniform = __all_sync(am, key == __shfl_sync(am, key, __ffs(am) - 1));
+                                             double si) {
   double A[9], B[9], Cm[9];
-  if (!uniform) {
-    if (planar >= 0) {
-      double a6[6], c6[6];
+  if (planar >= 0) {
+    double a6[6], c6[6];
 #pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        a6[k] = I.A[k];
-        c6[k] = I.C[k];
-      }
-      sym_planar(a6, planar, co, si);
-      sym_planar(c6, planar, co, si);
-      sym_expand(a6, A);
-      sym_expand(c6, Cm);
-#pragma unroll
-      for (int k = 0; k < 9; ++k) B[k] = I.B[k];
-      planar_rows(B, planar, co, si);
-      planar_cols(B, planar, co, si);
-    } else {
-      double a6[6], c6[6];
-      sym_rotate(Rr, I.A, a6);
-      sym_rotate(Rr, I.C, c6);
-      gen_rotate(Rr, I.B, B);
-      sym_expand(a6, A);
-      sym_expand(c6, Cm);
+    for (int k = 0; k < 6; ++k) {
+      a6[k] = I.A[k];
+      c6[k] = I.C[k];
     }
-    ABI o;
-    shift_general(A, B, Cm, t, o);
-    return o;
-  }
-  if (planar == 0) {
-    rotate_planar<0>(I, co, si, A, B, Cm);
-  } else if (planar == 1) {
-    rotate_planar<1>(I, co, si, A, B, Cm);
-  } else if (planar == 2) {
-    rotate_planar<2>(I, co, si, A, B, Cm);
+    sym_planar(a6, planar, co, si);
+    sym_planar(c6, planar, co, si);
+    sym_expand(a6, A);
+    sym_expand(c6, Cm);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) B[k] = I.B[k];
+    planar_rows(B, planar, co, si);
+    planar_cols(B, planar, co, si);
   } else {
     double a6[6], c6[6];
     sym_rotate(Rr, I.A, a6);
@@ -316,20 +228,7 @@ __device__ __forceinline__ ABI abi_to_parent(const ABI& I, const double* Rr, V3<
     sym_expand(c6, Cm);
   }
   ABI o;
-  if (taxis == 0) {
-    shift_axis<0>(A, B, Cm, t.x, o);
-  } else if (taxis == 1) {
-    shift_axis<1>(A, B, Cm, t.y, o);
-  } else if (taxis == 2) {
-    shift_axis<2>(A, B, Cm, t.z, o);
-  } else if (taxis == 3) {
-    sym_pack(A, o.A);
-    sym_pack(Cm, o.C);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) o.B[k] = B[k];
-  } else {
-    shift_general(A, B, Cm, t, o);
-  }
+  shift_general(A, B, Cm, t, o);
   return o;
 }
 
@@ -831,7 +730,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
           co = Rr[3 * i1 + i1];
           si = Rr[3 * i2 + i1];
         }
-        const ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si, bw_taxis(w1));
+        const ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si);
         if (pb == b - 1) {
           carryI = Ip;
         } else {

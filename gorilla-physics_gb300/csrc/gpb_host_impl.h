@@ -161,18 +161,7 @@ void fill_lane(const gpb_model* m, int64_t inst, const InstInfo& I, const PackDe
     if (t == GPB_JOINT_PRISMATIC && sk != 0.0) flags |= BF_SPRING;
     if (in[7] == 0.0 && in[8] == 0.0 && in[9] == 0.0) flags |= BF_DIAG_INERTIA;
     S.w(((P.topo + b) * 2) * L + l, (uint32_t)t | ((uint32_t)par << 4) | ((uint32_t)qo << 12) | ((uint32_t)vo << 22));
-    uint32_t taxis = 0;
-    if (t == GPB_JOINT_REVOLUTE || t == GPB_JOINT_FIXED) {
-      int nzt = 0, jt = 0;
-      for (int e = 0; e < 3; ++e)
-        if (iso[4 + e] != 0.0) {
-          nzt++;
-          jt = e;
-        }
-      if (nzt <= 1) taxis = BW_TAXIS | ((uint32_t)(nzt == 0 ? 3 : jt) << 25);
-    }
-    S.w(((P.topo + b) * 2 + 1) * L + l,
-        flags | ((uint32_t)cfirst[b] << 8) | ((uint32_t)ccount[b] << 16) | taxis);
+    S.w(((P.topo + b) * 2 + 1) * L + l, flags | ((uint32_t)cfirst[b] << 8) | ((uint32_t)ccount[b] << 16));
     double vals[TOPO_D];
     for (int e = 0; e < 9; ++e) vals[TD_RINIT + e] = R[e];
     for (int e = 0; e < 3; ++e) vals[TD_TINIT + e] = iso[4 + e];

@@ -25,11 +25,6 @@ enum BodyFlags : uint32_t {
   BF_DIAG_INERTIA = 1u << 7,       // body-frame moment is diagonal
 };
 __host__ __device__ inline uint32_t bf_axis_index(uint32_t flags) { return (flags >> 2) & 3u; }
-// Topology word 1, bits 24-26: the joint's translation is constant (fixed or
-// revolute joint) and lies along one axis: bit 24 set, bits 25-26 = the axis
-// (0-2), or 3 when the translation is zero.
-constexpr uint32_t BW_TAXIS = 1u << 24;
-__host__ __device__ inline int bw_taxis(uint32_t w1) { return (w1 & BW_TAXIS) ? (int)((w1 >> 25) & 3u) : -1; }
 
 // Doubles (and floats) of one body in the topology table.
 constexpr int TOPO_D = 28;  // Rinit (9, row-major), tinit (3), axis (3), inertia (10), spring (2), armature
