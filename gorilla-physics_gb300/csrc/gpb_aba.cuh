@@ -360,7 +360,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
   const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
   using V = V3<R>;
   using VD = V3<double>;
-  const bool contacts = c.nc > 0;
+  const bool contacts = c.nc > 0 || c.nu > 1;     // world poses in FP64 (points or cuboid pairs)
   const bool wide = contacts || sizeof(R) == 8;  // FP64 joint transforms
   const V zero{R(0), R(0), R(0)};
   V pw_ = zero, pv_ = zero;                  // parent velocity (chain carry)
@@ -561,6 +561,14 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
           }
         }
       }
+      const int uslot = (int)((w1 >> W1_CUBOID_SHIFT) & 15u);
+      if (uslot && c.nu > 1) {  // cuboid record: world pose, world twist about the origin
+        const bool root6 = type == 3 && parent == 0;
+        const VD omd = root6 ? VD{v[vo], v[vo + 1], v[vo + 2]} : VD{double(om.x), double(om.y), double(om.z)};
+        const VD vld = root6 ? VD{v[vo + 3], v[vo + 4], v[vo + 5]} : VD{double(vl.x), double(vl.y), double(vl.z)};
+        const VD omw = mul(Rw, omd);
+        store_cuboid(c, uslot - 1, b, Rw, posw, omw, mul(Rw, vld) - cross(omw, posw));
+      }
     }
     // records for the inward and second outward passes
 #pragma unroll
@@ -593,6 +601,14 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     pv_ = vl;
     ppos = posw;
     pR = Rw;
+  }
+  // ---- cuboid pairs: p −= W (body frame, FP64 records of contact mechanisms)
+  if (c.nu > 1) {
+    st |= lane_cuboid_pairs(c);
+    for (int b = 0; b < c.nb; ++b) {
+      const int uslot = (int)((c.w(2 * b + 1) >> W1_CUBOID_SHIFT) & 15u);
+      if (uslot) store_svd(c, c.L.F + 6 * b, load_svd(c, c.L.F + 6 * b) - cuboid_wrench_body(c, uslot - 1));
+    }
   }
   // ---- pass 2 (inward): articulated inertias and bias forces --------------
   // A child that is the next body (every link of a chain) hands its terms to

@@ -63,7 +63,7 @@ struct EvalCoop {
   __device__ int run(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x, bool alive) const {
     Col<double> none{nullptr};
     int st = 0;
-    if (alive) lane_sweeps<R, RC>(c, q, v, t, ht, none, false);
+    if (alive) st |= lane_sweeps<R, RC>(c, q, v, t, ht, none, false);
     sh->alive[c.lane] = alive ? 1 : 0;
     coop_bar();  // A: sweeps done, composite inertias and rhs in scratch
     if (alive) {

@@ -128,7 +128,18 @@ int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
   I.model = m->contact_model ? m->contact_model[i] : GPB_HUNT_CROSSLEY;
   if (I.model != GPB_HUNT_CROSSLEY && I.model != GPB_LINEAR_SPRING_DAMPER)
     return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": bad contact model");
-  sig = (sig ^ (uint64_t)(I.nc * 7 + I.nh)) * 1099511628211ull;
+  // cuboid colliders (src/rigid_body.rs:197-199): sizes all zero = none
+  I.nu = 0;
+  for (int b = 0; b < I.nb && m->body_cuboid; ++b) {
+    const double* d = m->body_cuboid + 3 * (size_t)(I.j0 + b);
+    if (d[0] == 0.0 && d[1] == 0.0 && d[2] == 0.0) continue;
+    if (!(d[0] > 0.0 && d[1] > 0.0 && d[2] > 0.0 && std::isfinite(d[0] + d[1] + d[2])))
+      return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": cuboid sizes must be positive");
+    if (++I.nu > GPB_MAX_CUBOIDS)
+      return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": more than " +
+                                   std::to_string(GPB_MAX_CUBOIDS) + " cuboid colliders");
+  }
+  sig = (sig ^ (uint64_t)(I.nc * 7 + I.nh + 1000 * I.nu)) * 1099511628211ull;
   I.sig = sig;
   return GPB_OK;
 }
@@ -186,6 +197,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
       P.nv = std::max(P.nv, I.nv);
       P.nc = std::max(P.nc, I.nc);
       P.nh = std::max(P.nh, I.nh);
+      P.nu = std::max(P.nu, I.nu);
       P.minnv = std::min(P.minnv, I.nv);
       if (!I.chain) P.chain = 0;
     }
@@ -202,7 +214,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
     rq += P.nq;
     rv += P.nv;
     rl += LANE_I;
-    rs += scratch_layout(P.nb, P.nq, P.nv, P.nc).total;
+    rs += scratch_layout(P.nb, P.nq, P.nv, P.nc, P.nu).total;
   }
   const size_t L = LANES;
   std::vector<uint32_t> W(rt * 2 * L, 0);
@@ -684,6 +696,55 @@ extern "C" int gpb_dynamics_static(gpb_batch* b, const double* q, const double* 
                                   qdd, s));
   b->ctx->launches++;
   return GPB_OK;
+}
+
+extern "C" int gpb_collide_cuboids_device(gpb_ctx* ctx, int64_t n, const double* pose_a, const double* size_a,
+                                          const double* pose_b, const double* size_b, int32_t* result,
+                                          double* cp_a, double* cp_b, void* stream) {
+  if (!ctx || n < 0) return fail(GPB_E_INVAL, "gpb_collide_cuboids_device: bad argument");
+  if (n == 0) return GPB_OK;
+  if (!pose_a || !size_a || !pose_b || !size_b || !result || !cp_a || !cp_b)
+    return fail(GPB_E_INVAL, "gpb_collide_cuboids_device: NULL buffer");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  CUDA_TRY(launch_collide(n, pose_a, size_a, pose_b, size_b, result, cp_a, cp_b, ctx->num_sms, s));
+  ctx->launches++;
+  return GPB_OK;
+}
+
+extern "C" int gpb_collide_cuboids(gpb_ctx* ctx, int64_t n, const double* pose_a, const double* size_a,
+                                   const double* pose_b, const double* size_b, int32_t* result, double* cp_a,
+                                   double* cp_b) {
+  if (!ctx || n < 0) return fail(GPB_E_INVAL, "gpb_collide_cuboids: bad argument");
+  if (n == 0) return GPB_OK;
+  if (!pose_a || !size_a || !pose_b || !size_b || !result || !cp_a || !cp_b)
+    return fail(GPB_E_INVAL, "gpb_collide_cuboids: NULL buffer");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  // one allocation: poses (14 n), sizes (6 n), contact points (6 n), results (n int32)
+  DBuf<double> d;
+  if (d.alloc((size_t)n * 26 + ((size_t)n + 1) / 2) != cudaSuccess)
+    return fail(GPB_E_NOMEM, "gpb_collide_cuboids: device allocation failed");
+  double *pa = d.p, *pb = pa + 7 * n, *sa = pb + 7 * n, *sb = sa + 3 * n, *ca = sb + 3 * n, *cb = ca + 3 * n;
+  int32_t* res = reinterpret_cast<int32_t*>(cb + 3 * n);
+  cudaStream_t s = ctx->stream;
+  int rc = GPB_OK;
+  auto h2d = [&](double* dst, const double* src, int64_t k) {
+    return cudaMemcpyAsync(dst, src, (size_t)k * sizeof(double), cudaMemcpyHostToDevice, s);
+  };
+  cudaError_t e = h2d(pa, pose_a, 7 * n);
+  if (e == cudaSuccess) e = h2d(pb, pose_b, 7 * n);
+  if (e == cudaSuccess) e = h2d(sa, size_a, 3 * n);
+  if (e == cudaSuccess) e = h2d(sb, size_b, 3 * n);
+  if (e == cudaSuccess) e = launch_collide(n, pa, sa, pb, sb, res, ca, cb, ctx->num_sms, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cp_a, ca, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cp_b, cb, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(result, res, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) rc = fail(GPB_E_CUDA, std::string("gpb_collide_cuboids: ") + cudaGetErrorString(e));
+  ctx->launches++;
+  cudaStreamSynchronize(s);
+  d.free();
+  return rc;
 }
 
 extern "C" double gpb_open_loop_tau(uint32_t seed, int64_t instance, int64_t block, int32_t dof,

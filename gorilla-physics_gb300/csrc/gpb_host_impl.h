@@ -54,7 +54,7 @@ struct DBuf {
 
 // Validated shape of one instance of a gpb_model.
 struct InstInfo {
-  int32_t j0, nb, nq, nv, c0, nc, h0, nh, model;
+  int32_t j0, nb, nq, nv, c0, nc, h0, nh, model, nu;
   bool chain;
   uint64_t sig;  // topology class
 };
@@ -103,6 +103,7 @@ void fill_lane(const gpb_model* m, int64_t inst, const InstInfo& I, const PackDe
   S.li(li + 4 * L, I.nc);
   S.li(li + 5 * L, I.nh);
   S.li(li + 6 * L, I.model);
+  S.li(li + 7 * L, I.nu);
   // contacts sorted by body (stable), remembering the user order
   std::vector<int> corder(I.nc);
   std::iota(corder.begin(), corder.end(), 0);
@@ -134,9 +135,11 @@ void fill_lane(const gpb_model* m, int64_t inst, const InstInfo& I, const PackDe
     const int par = m->joint_parent[I.j0 + b];  // 1-based
     if (par >= 1 && par != b) branch[par - 1] = true;
   }
-  int qo = 0, vo = 0;
+  int qo = 0, vo = 0, slot = 0;
   for (int b = 0; b < I.nb; ++b) {
     const int j = I.j0 + b;
+    const double* cub = m->body_cuboid ? m->body_cuboid + 3 * (size_t)j : nullptr;
+    const bool has_cub = cub && !(cub[0] == 0.0 && cub[1] == 0.0 && cub[2] == 0.0);
     const int t = m->joint_type[j], par = m->joint_parent[j];
     const double* iso = m->joint_iso + 7 * (size_t)j;
     const double* ax = m->joint_axis + 3 * (size_t)j;
@@ -161,7 +164,11 @@ void fill_lane(const gpb_model* m, int64_t inst, const InstInfo& I, const PackDe
     if (t == GPB_JOINT_PRISMATIC && sk != 0.0) flags |= BF_SPRING;
     if (in[7] == 0.0 && in[8] == 0.0 && in[9] == 0.0) flags |= BF_DIAG_INERTIA;
     S.w(((P.topo + b) * 2) * L + l, (uint32_t)t | ((uint32_t)par << 4) | ((uint32_t)qo << 12) | ((uint32_t)vo << 22));
-    S.w(((P.topo + b) * 2 + 1) * L + l, flags | ((uint32_t)cfirst[b] << 8) | ((uint32_t)ccount[b] << 16));
+    // cuboid slots in body order: the pairs are then visited in the reference's
+    // order (src/contact.rs:191-197)
+    const uint32_t uslot = has_cub ? (uint32_t)(++slot) : 0u;
+    S.w(((P.topo + b) * 2 + 1) * L + l, flags | ((uint32_t)cfirst[b] << 8) | ((uint32_t)ccount[b] << 16) |
+                                             (uslot << W1_CUBOID_SHIFT));
     double vals[TOPO_D];
     for (int e = 0; e < 9; ++e) vals[TD_RINIT + e] = R[e];
     for (int e = 0; e < 3; ++e) vals[TD_TINIT + e] = iso[4 + e];
@@ -170,6 +177,7 @@ void fill_lane(const gpb_model* m, int64_t inst, const InstInfo& I, const PackDe
     vals[TD_SPRING] = sk;
     vals[TD_SPRING + 1] = sl;
     vals[TD_ARMATURE] = m->joint_armature ? m->joint_armature[j] : 0.0;
+    for (int e = 0; e < 3; ++e) vals[TD_CUBOID + e] = has_cub ? cub[e] : 0.0;
     for (int e = 0; e < TOPO_D; ++e) S.td((P.topo * TOPO_D + TOPO_D * b + e) * L + l, vals[e]);
     // state maps and the zero state (identity pose for floating joints)
     for (int e = 0; e < joint_nq(t); ++e) S.qmap((P.q + qo + e) * L + l, q_user + qo + e);

@@ -27,14 +27,26 @@ enum BodyFlags : uint32_t {
 __host__ __device__ inline uint32_t bf_axis_index(uint32_t flags) { return (flags >> 2) & 3u; }
 
 // Doubles (and floats) of one body in the topology table.
-constexpr int TOPO_D = 28;  // Rinit (9, row-major), tinit (3), axis (3), inertia (10), spring (2), armature
-constexpr int TD_RINIT = 0, TD_TINIT = 9, TD_AXIS = 12, TD_INERTIA = 15, TD_SPRING = 25, TD_ARMATURE = 27;
+// Rinit (9, row-major), tinit (3), axis (3), inertia (10), spring (2), armature,
+// cuboid collider sizes (3)
+constexpr int TOPO_D = 31;
+constexpr int TD_RINIT = 0, TD_TINIT = 9, TD_AXIS = 12, TD_INERTIA = 15, TD_SPRING = 25, TD_ARMATURE = 27,
+              TD_CUBOID = 28;
+// Second topology word: flags (bits 0-7), first contact (8-15), contact count
+// (16-23), cuboid slot + 1 (24-27; 0 = no collider).
+constexpr int W1_CUBOID_SHIFT = 24;
+// Per-slot cuboid record in scratch (FP64 rows): world rotation (9), centre (3),
+// world twist about the world origin (ω 3, v 3), sizes (3), accumulated world
+// wrench about the world origin (moment 3, force 3).
+constexpr int UREC_D = 27;
+constexpr int UR_R = 0, UR_T = 9, UR_W = 12, UR_V = 15, UR_DIM = 18, UR_MOM = 21, UR_FRC = 24;
 constexpr int CTC_D = 6;    // location (3), k, radius, damping
 constexpr int HS_D = 8;     // point (3), normal (3), alpha, mu
-constexpr int LANE_I = 8;   // per-lane ints: instance, nb, nq, nv, nc, nh, contact model, pad
+constexpr int LANE_I = 8;   // per-lane ints: instance, nb, nq, nv, nc, nh, contact model, cuboids
 
 struct PackDesc {
   int32_t count, nb, nq, nv, nc, nh, chain, minnv;  // minnv: smallest DOF count of its lanes
+  int32_t nu, pad_;  // nu: largest cuboid-collider count of its lanes
   // bases in rows (one row = LANES elements)
   int64_t topo;   // topology bodies (2 int words / TOPO_D reals per body)
   int64_t ctc;    // contacts
@@ -47,9 +59,9 @@ struct PackDesc {
 // Scratch sub-array offsets (rows of 8-byte words; R-typed arrays use the same
 // row pitch so that the float and double kernels share one layout).
 struct ScratchLayout {
-  int32_t X, V, A, S, I, F, C, AI, DU, RF, M, D, rhs, q0, v0, qs, vs, facc, tau, cf, total;
+  int32_t X, V, A, S, I, F, C, AI, DU, RF, M, D, rhs, q0, v0, qs, vs, facc, tau, cf, U, total;
 };
-__host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, int nc) {
+__host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, int nc, int nu) {
   ScratchLayout s;
   int o = 0;
   s.X = o; o += 12 * nb;
@@ -73,6 +85,7 @@ __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, 
   s.facc = o; o += nv;
   s.tau = o; o += nv;
   s.cf = o; o += 3 * nc;
+  s.U = o; o += nu > 1 ? UREC_D * nu : 0;  // cuboid records (pairs need two)
   s.total = o;
   return s;
 }
@@ -179,6 +192,11 @@ cudaError_t launch_scatter_words(const ScatterTable& table, const uint64_t* key,
 // dst[k] = src[idx[k]] for 4- or 8-byte elements.
 cudaError_t launch_gather_words(const void* src, int bytes, const int64_t* idx, int64_t n, void* dst,
                                 cudaStream_t s);
+// gpb_collide_cuboids: n cuboid pairs (device arrays; pose 7 / sizes 3 doubles
+// per cuboid), one thread per pair.
+cudaError_t launch_collide(int64_t n, const double* pose_a, const double* size_a, const double* pose_b,
+                           const double* size_b, int32_t* result, double* cp_a, double* cp_b, int num_sms,
+                           cudaStream_t s);
 // gpb_dynamics_static: the dynamics kernel with its scratch in the library's
 // static device array (cudaErrorInvalidValue if scratch_words exceeds it).
 cudaError_t launch_dynamics_static(const DeviceBatch& b, int device, int64_t scratch_words,

@@ -25,6 +25,7 @@
 #include "gpb_device.cuh"
 #include "gpb_internal.h"
 #include "gpb_rng.h"
+#include "gpb_collide.cuh"
 
 namespace gpb {
 
@@ -66,6 +67,7 @@ struct RealTopo<float> {
 template <typename R>
 struct LaneCtx {
   int lane, nb, nq, nv, nc, nh, model, chain;
+  int nu;       // cuboid colliders (slots 1..nu in body order)
   int springs;  // prismatic springs act (off for Articulated::free_velocity)
   double grav;  // gravitational acceleration along −z
   const uint32_t* W;  // topology words (row base applied, lane applied)
@@ -192,6 +194,143 @@ __device__ __forceinline__ V3<R> contact_force(int model, R z, V3<R> n, V3<R> ve
     f = f + vt * g;
   }
   return f;
+}
+
+// ---------------------------------------------------------------------------
+// Cuboid colliders (src/contact.rs:191-242).  The outward sweep of each
+// dynamics form writes a record per cuboid body (store_cuboid); after it,
+// lane_cuboid_pairs runs GJK/EPA on every pair and leaves each body's world
+// contact wrench in its record; the form then subtracts that wrench from the
+// body's force before its inward sweep.
+
+// World pose, world twist about the world origin (the reference's `twists`)
+// and sizes of the cuboid of body b, into slot `slot`.
+template <typename R>
+__device__ __forceinline__ void store_cuboid(const LaneCtx<R>& c, int slot, int b, const M3<double>& Rw,
+                                             V3<double> p, V3<double> om, V3<double> v0) {
+  const int u = c.L.U + UREC_D * slot;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) c.d(u + UR_R + k) = Rw.a[k];
+  c.d(u + UR_T) = p.x;
+  c.d(u + UR_T + 1) = p.y;
+  c.d(u + UR_T + 2) = p.z;
+  c.d(u + UR_W) = om.x;
+  c.d(u + UR_W + 1) = om.y;
+  c.d(u + UR_W + 2) = om.z;
+  c.d(u + UR_V) = v0.x;
+  c.d(u + UR_V + 1) = v0.y;
+  c.d(u + UR_V + 2) = v0.z;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) c.d(u + UR_DIM + k) = c.td(TOPO_D * b + TD_CUBOID + k);
+}
+template <typename R>
+__device__ __forceinline__ V3<double> rec3(const LaneCtx<R>& c, int e) {
+  return {c.d(e), c.d(e + 1), c.d(e + 2)};
+}
+
+// calculate_contact_force_collider (src/contact.rs:306-317): Hunt–Crossley
+// with k = 5e3 on both shapes, α = 1, μ = 1 (src/contact.rs:260-302); the force
+// from B on A.  A zero-depth contact gives a NaN normal, as
+// UnitVector3::new_normalize of a zero vector does (the instance then stops as
+// non-finite).
+__device__ __forceinline__ V3<double> collider_force(V3<double> pa, V3<double> pb, V3<double> vel) {
+  const V3<double> pen = pb - pa;
+  const double z = sqrt(dot(pen, pen));
+  const V3<double> n{pen.x / z, pen.y / z, pen.z / z};
+  const double zdot = -dot(vel, n);
+  const double k = 5e3 * 5e3 / (5e3 + 5e3);
+  const double zn = z * sqrt(z);
+  const double pi = fmax(1.5 * 1.0 * k * zn * zdot + k * zn, 0.0);
+  V3<double> f = n * pi;
+  const V3<double> vt = vel + n * zdot;
+  const double vtn = sqrt(dot(vt, vt));
+  if (vtn != 0.0) {
+    const double sl = vtn / 1e-3;
+    const double mue = sl > 1.0 ? 1.0 : sl;
+    f = f + vt * (-mue * pi / vtn);
+  }
+  return f;
+}
+
+// Every pair (i < j in body order) of this lane's cuboids through GJK/EPA
+// (CollisionDetector, src/collision/mod.rs:48-87); a hit pushes f on the first
+// body at its contact point and −f on the second at its own.  Returns
+// GPB_ST_COLLISION if a query met a case the reference panics on or ran past
+// its storage bounds.
+template <typename R>
+__device__ __noinline__ int lane_cuboid_pairs(const LaneCtx<R>& cin) {
+  const LaneCtx<R> c = cin;
+  const int U = c.L.U;
+  for (int s = 0; s < c.nu; ++s)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) c.d(U + UREC_D * s + UR_MOM + k) = 0.0;
+  int st = 0;
+  for (int a = 0; a + 1 < c.nu; ++a) {
+    const int ua = U + UREC_D * a;
+    gcol::BoxPose A;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) A.R[k] = c.d(ua + UR_R + k);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      A.t[k] = c.d(ua + UR_T + k);
+      A.dims[k] = c.d(ua + UR_DIM + k);
+    }
+    for (int b = a + 1; b < c.nu; ++b) {
+      const int ub = U + UREC_D * b;
+      gcol::BoxPose B;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) B.R[k] = c.d(ub + UR_R + k);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        B.t[k] = c.d(ub + UR_T + k);
+        B.dims[k] = c.d(ub + UR_DIM + k);
+      }
+      gcol::D3 ca, cb;
+      const int r = gcol::collide(A, B, true, &ca, &cb);
+      if (r < 0) {
+        st |= GPB_ST_COLLISION;
+        continue;
+      }
+      if (r != gcol::CG_HIT) continue;
+      const V3<double> pa{ca.x, ca.y, ca.z}, pb{cb.x, cb.y, cb.z};
+      const V3<double> va = rec3(c, ua + UR_V) + cross(rec3(c, ua + UR_W), pa);  // Twist::point_velocity
+      const V3<double> vb = rec3(c, ub + UR_V) + cross(rec3(c, ub + UR_W), pb);
+      const V3<double> f = collider_force(pa, pb, va - vb);
+      const V3<double> fm = f * -1.0;
+      const V3<double> ma = rec3(c, ua + UR_MOM) + cross(pa, f), fa = rec3(c, ua + UR_FRC) + f;
+      const V3<double> mb = rec3(c, ub + UR_MOM) + cross(pb, fm), fb = rec3(c, ub + UR_FRC) + fm;
+      c.d(ua + UR_MOM) = ma.x;
+      c.d(ua + UR_MOM + 1) = ma.y;
+      c.d(ua + UR_MOM + 2) = ma.z;
+      c.d(ua + UR_FRC) = fa.x;
+      c.d(ua + UR_FRC + 1) = fa.y;
+      c.d(ua + UR_FRC + 2) = fa.z;
+      c.d(ub + UR_MOM) = mb.x;
+      c.d(ub + UR_MOM + 1) = mb.y;
+      c.d(ub + UR_MOM + 2) = mb.z;
+      c.d(ub + UR_FRC) = fb.x;
+      c.d(ub + UR_FRC + 1) = fb.y;
+      c.d(ub + UR_FRC + 2) = fb.z;
+    }
+  }
+  return st;
+}
+
+// The world wrench (moment about the world origin, force) that the cuboid
+// pairs exert on the body of slot `slot`, in the body frame with the moment
+// about the body origin: (Rᵀ(m − p × f), Rᵀ f).
+template <typename R>
+__device__ __forceinline__ SV<double> cuboid_wrench_body(const LaneCtx<R>& c, int slot) {
+  const int u = c.L.U + UREC_D * slot;
+  M3<double> Rw;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Rw.a[k] = c.d(u + UR_R + k);
+  const V3<double> p = rec3(c, u + UR_T), m = rec3(c, u + UR_MOM), f = rec3(c, u + UR_FRC);
+  const V3<double> mo = m - cross(p, f);
+  return {{Rw.a[0] * mo.x + Rw.a[3] * mo.y + Rw.a[6] * mo.z, Rw.a[1] * mo.x + Rw.a[4] * mo.y + Rw.a[7] * mo.z,
+           Rw.a[2] * mo.x + Rw.a[5] * mo.y + Rw.a[8] * mo.z},
+          {Rw.a[0] * f.x + Rw.a[3] * f.y + Rw.a[6] * f.z, Rw.a[1] * f.x + Rw.a[4] * f.y + Rw.a[7] * f.z,
+           Rw.a[2] * f.x + Rw.a[5] * f.y + Rw.a[8] * f.z}};
 }
 
 // Offset of H(i, j), i ≥ j, in the tile-major packed lower triangle: 4×4 tiles
@@ -411,10 +550,11 @@ __device__ __noinline__ void lane_solve(const LaneCtx<R>& cin) {
 // kinematics, twists, bias accelerations, contacts and Newton–Euler outward;
 // composite inertias and joint forces inward.  Leaves each body's composite
 // inertia in the I region, the motion subspaces in S and τ + τ_spring − c in
-// rhs (in the factor's precision RC).
+// rhs (in the factor's precision RC).  Returns GPB_ST_COLLISION if a cuboid
+// pair query failed, else 0.
 template <typename R, typename RC>
-__device__ __noinline__ void lane_sweeps(const LaneCtx<R>& cin, Col<double> q, Col<double> v, Col<double> tau,
-                                         bool have_tau, Col<double> cforce, bool want_cf) {
+__device__ __noinline__ int lane_sweeps(const LaneCtx<R>& cin, Col<double> q, Col<double> v, Col<double> tau,
+                                        bool have_tau, Col<double> cforce, bool want_cf) {
   const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
   const R g = R(c.grav);
   // ---- outward sweep --------------------------------------------------
@@ -577,6 +717,15 @@ __device__ __noinline__ void lane_sweeps(const LaneCtx<R>& cin, Col<double> q, C
     }
     store_si(c, c.L.I + 10 * b, Iw);
     store_sv(c, c.L.F + 6 * b, f);
+    const int uslot = (int)((w1 >> W1_CUBOID_SHIFT) & 15u);
+    if (uslot && c.nu > 1) {
+      M3<double> Rd;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Rd.a[k] = double(Rb.a[k]);
+      store_cuboid(c, uslot - 1, b, Rd, V3<double>{double(pb.x), double(pb.y), double(pb.z)},
+                   V3<double>{double(Vb.w.x), double(Vb.w.y), double(Vb.w.z)},
+                   V3<double>{double(Vb.v.x), double(Vb.v.y), double(Vb.v.z)});
+    }
     if (fl & BF_BRANCH) {
 #pragma unroll
       for (int k = 0; k < 9; ++k) c.r(c.L.X + 12 * b + k) = Rb.a[k];
@@ -590,6 +739,20 @@ __device__ __noinline__ void lane_sweeps(const LaneCtx<R>& cin, Col<double> q, C
     pp = pb;
     Vp = Vb;
     Ap = Ab;
+  }
+  // ---- cuboid pairs: f −= W (world frame, about the world origin) ------
+  int st = 0;
+  if (c.nu > 1) {
+    st = lane_cuboid_pairs(c);
+    for (int b = 0; b < c.nb; ++b) {
+      const int uslot = (int)((c.w(2 * b + 1) >> W1_CUBOID_SHIFT) & 15u);
+      if (!uslot) continue;
+      const int u = c.L.U + UREC_D * (uslot - 1);
+      const SV<R> f = load_sv(c, c.L.F + 6 * b);
+      const SV<R> W{{R(c.d(u + UR_MOM)), R(c.d(u + UR_MOM + 1)), R(c.d(u + UR_MOM + 2))},
+                    {R(c.d(u + UR_FRC)), R(c.d(u + UR_FRC + 1)), R(c.d(u + UR_FRC + 2))}};
+      store_sv(c, c.L.F + 6 * b, f - W);
+    }
   }
 
   // ---- inward sweep: composite inertia, joint forces ------------------
@@ -636,6 +799,7 @@ __device__ __noinline__ void lane_sweeps(const LaneCtx<R>& cin, Col<double> q, C
       ctarget = -1;
     }
   }
+  return st;
 }
 
 // CRBA fill of the rows of H in the tile rows I with I mod nw == w (all rows
@@ -690,9 +854,9 @@ __device__ __noinline__ void lane_fill(const LaneCtx<R>& cin, int w, int nw) {
 template <typename R, typename RC>
 __device__ __noinline__ int lane_dynamics(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<double> tau,
                                           bool have_tau, Col<double> qdd, Col<double> cforce, bool want_cf) {
-  lane_sweeps<R, RC>(c, q, v, tau, have_tau, cforce, want_cf);
+  const int st = lane_sweeps<R, RC>(c, q, v, tau, have_tau, cforce, want_cf);
   lane_fill<R, RC>(c, 0, 1);
-  return lane_cholesky_solve<R, RC>(c, qdd);
+  return st | lane_cholesky_solve<R, RC>(c, qdd);
 }
 
 #include "gpb_link.cuh"
@@ -712,7 +876,7 @@ __device__ __forceinline__ int refine(const LaneCtx<float>& c, const LaneCtx<dou
                                       Col<double> cf, bool want_cf) {
   int st = 0;
   for (int it = 0; it < 2; ++it) {
-    lane_link<double, RC, true>(c2, q, v, tau, have_tau, qdd, qdd, cf, want_cf && it == 0);
+    st |= lane_link<double, RC, true>(c2, q, v, tau, have_tau, qdd, qdd, cf, want_cf && it == 0);
     lane_solve<float, RC>(c);
     double dmax = 0.0, xmax = 1.0;
     for (int i = 0; i < c.nv; ++i) {
@@ -885,6 +1049,7 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   c.nc = b.plain ? 0 : li[4 * LANES];  // free_velocity: no contact points
   c.nh = li[5 * LANES];
   c.model = li[6 * LANES];
+  c.nu = b.plain ? 0 : li[7 * LANES];  // free_velocity: no colliders
   c.chain = pd.chain;
   c.springs = b.plain ? 0 : 1;
   c.grav = b.gravity;
@@ -896,7 +1061,7 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   c.TDD = b.topoD + pd.topo * TOPO_D * LANES + lane;
   c.CDD = b.ctcD + pd.ctc * CTC_D * LANES + lane;
   c.HDD = b.hsD + pd.hs * HS_D * LANES + lane;
-  c.L = scratch_layout(pd.nb, pd.nq, pd.nv, pd.nc);
+  c.L = scratch_layout(pd.nb, pd.nq, pd.nv, pd.nc, pd.nu);
   c.sD = b.scratch + pd.scr * LANES + lane;
   c.sR = reinterpret_cast<R*>(b.scratch + pd.scr * LANES) + lane;
   c.s0 = reinterpret_cast<char*>(b.scratch + pd.scr * LANES);
@@ -1116,6 +1281,44 @@ cudaError_t launch_gather_words(const void* src, int bytes, const int64_t* idx, 
     gather_words_kernel<uint64_t><<<g, 256, 0, s>>>((const uint64_t*)src, idx, n, (uint64_t*)dst);
   else
     gather_words_kernel<uint32_t><<<g, 256, 0, s>>>((const uint32_t*)src, idx, n, (uint32_t*)dst);
+  return cudaGetLastError();
+}
+
+// CollisionDetector queries of independent cuboid pairs, one thread per pair.
+__global__ void __launch_bounds__(128) collide_kernel(int64_t n, const double* __restrict__ pa,
+                                                      const double* __restrict__ sa, const double* __restrict__ pb,
+                                                      const double* __restrict__ sb, int32_t* __restrict__ result,
+                                                      double* __restrict__ ca, double* __restrict__ cb) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    gcol::BoxPose A, B;
+    gcol::quat_to_matrix(pa[7 * i], pa[7 * i + 1], pa[7 * i + 2], pa[7 * i + 3], A.R);
+    gcol::quat_to_matrix(pb[7 * i], pb[7 * i + 1], pb[7 * i + 2], pb[7 * i + 3], B.R);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      A.t[k] = pa[7 * i + 4 + k];
+      B.t[k] = pb[7 * i + 4 + k];
+      A.dims[k] = sa[3 * i + k];
+      B.dims[k] = sb[3 * i + k];
+    }
+    gcol::D3 x{0.0, 0.0, 0.0}, y{0.0, 0.0, 0.0};
+    const int r = gcol::collide(A, B, true, &x, &y);
+    result[i] = r;
+    if (r != gcol::CG_HIT) x = y = gcol::D3{0.0, 0.0, 0.0};
+    ca[3 * i] = x.x;
+    ca[3 * i + 1] = x.y;
+    ca[3 * i + 2] = x.z;
+    cb[3 * i] = y.x;
+    cb[3 * i + 1] = y.y;
+    cb[3 * i + 2] = y.z;
+  }
+}
+
+cudaError_t launch_collide(int64_t n, const double* pose_a, const double* size_a, const double* pose_b,
+                           const double* size_b, int32_t* result, double* cp_a, double* cp_b, int num_sms,
+                           cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n + 127) / 128, (int64_t)std::max(num_sms, 1) * 16);
+  collide_kernel<<<(unsigned)blocks, 128, 0, s>>>(n, pose_a, size_a, pose_b, size_b, result, cp_a, cp_b);
   return cudaGetLastError();
 }
 

@@ -54,14 +54,15 @@ __device__ __forceinline__ void load_rel(const LaneCtx<R>& c, int b, M3<R>& Rr, 
 }
 
 // RESIDUAL = false: q̈ into qdd (returns status bits).  RESIDUAL = true: the
-// residual at ẍ = xacc into the scratch rhs vector (in RC), returns 0.
+// residual at ẍ = xacc into the scratch rhs vector (in RC), returns the
+// cuboid-collision status.
 template <typename R, typename RC, bool RESIDUAL>
 __device__ __noinline__ int lane_link(const LaneCtx<R>& cin, Col<double> q, Col<double> v,
                                       Col<double> tau, bool have_tau, Col<double> xacc,
                                       Col<double> qdd, Col<double> cf, bool want_cf) {
   const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
   using V = V3<R>;
-  const bool contacts = c.nc > 0;
+  const bool contacts = c.nc > 0 || c.nu > 1;  // world poses (points or cuboid pairs)
   const V zero{R(0), R(0), R(0)};
   V pw_ = zero, pv_ = zero, pal_ = zero, pa_ = zero, ppos = zero;
   M3<R> pR = eye3<R>();
@@ -210,6 +211,16 @@ __device__ __noinline__ int lane_link(const LaneCtx<R>& cin, Col<double> q, Col<
           }
         }
       }
+      const int uslot = (int)((w1 >> W1_CUBOID_SHIFT) & 15u);
+      if (uslot && c.nu > 1) {  // cuboid record: world pose, world twist about the origin
+        M3<double> Rd;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Rd.a[k] = double(Rw.a[k]);
+        const V3<double> pd{double(posw.x), double(posw.y), double(posw.z)};
+        const V3<double> omw = mul(Rd, V3<double>{double(om.x), double(om.y), double(om.z)});
+        const V3<double> vlw = mul(Rd, V3<double>{double(vl.x), double(vl.y), double(vl.z)});
+        store_cuboid(c, uslot - 1, b, Rd, pd, omw, vlw - cross(omw, pd));
+      }
     }
     store_sv(c, c.L.F + 6 * b, f);
 #pragma unroll
@@ -238,6 +249,18 @@ __device__ __noinline__ int lane_link(const LaneCtx<R>& cin, Col<double> q, Col<
     pa_ = ac;
     ppos = posw;
     pR = Rw;
+  }
+  // ---- cuboid pairs: f −= W (body frame) ----------------------------
+  int st = 0;
+  if (c.nu > 1) {
+    st = lane_cuboid_pairs(c);
+    for (int b = 0; b < c.nb; ++b) {
+      const int uslot = (int)((c.w(2 * b + 1) >> W1_CUBOID_SHIFT) & 15u);
+      if (!uslot) continue;
+      const SV<double> W = cuboid_wrench_body(c, uslot - 1);
+      const SV<R> Wr{{R(W.w.x), R(W.w.y), R(W.w.z)}, {R(W.v.x), R(W.v.y), R(W.v.z)}};
+      store_sv(c, c.L.F + 6 * b, load_sv(c, c.L.F + 6 * b) - Wr);
+    }
   }
   // ---- inward: joint forces, composite inertias, mass-matrix fill ------
   const int nv = c.nv;
@@ -340,6 +363,6 @@ __device__ __noinline__ int lane_link(const LaneCtx<R>& cin, Col<double> q, Col<
       ctarget = -1;
     }
   }
-  if (RESIDUAL) return 0;
-  return lane_cholesky_solve<R, RC>(cin, qdd);
+  if (RESIDUAL) return st;
+  return st | lane_cholesky_solve<R, RC>(cin, qdd);
 }

@@ -56,7 +56,7 @@ struct OwnedModel {
   std::vector<int32_t> joint_offset{0, 0}, joint_type, joint_parent, contact_offset{0, 0}, contact_body,
       halfspace_offset{0, 0}, contact_model;
   std::vector<double> joint_iso, joint_axis, joint_spring, body_inertia, contact_params, halfspace_params,
-      joint_armature;
+      joint_armature, body_cuboid;
   gpb_model view() const {
     gpb_model m;
     std::memset(&m, 0, sizeof(m));
@@ -75,6 +75,7 @@ struct OwnedModel {
     m.halfspace_params = halfspace_params.data();
     m.contact_model = contact_model.data();
     m.joint_armature = joint_armature.data();
+    m.body_cuboid = body_cuboid.data();
     return m;
   }
 };
@@ -99,7 +100,8 @@ struct Result {
 // Device bytes of one pack with these capacities (every per-slot array of the pool).
 int64_t pack_bytes(const gpb_slot_class& c) {
   const int64_t L = LANES;
-  const int64_t nb = c.max_bodies, nq = c.max_q, nv = c.max_v, nc = c.max_contacts, nh = c.max_halfspaces;
+  const int64_t nb = c.max_bodies, nq = c.max_q, nv = c.max_v, nc = c.max_contacts, nh = c.max_halfspaces,
+                nu = c.max_cuboids;
   int64_t b = 0;
   b += nb * 2 * L * 4;                                     // topology words
   b += nb * TOPO_D * L * (8 + 4);                          // topology reals (double + float)
@@ -107,7 +109,7 @@ int64_t pack_bytes(const gpb_slot_class& c) {
   b += nh * HS_D * L * (8 + 4);                            // half-spaces
   b += LANE_I * L * 4;                                     // lane ints
   b += (nq + 2 * nv) * L * 8;                              // q, v, tau_in
-  b += (int64_t)scratch_layout((int)nb, (int)nq, (int)nv, (int)nc).total * L * 8;  // scratch
+  b += (int64_t)scratch_layout((int)nb, (int)nq, (int)nv, (int)nc, (int)nu).total * L * 8;  // scratch
   b += L * (4 + 8 + 4 + (int64_t)sizeof(LaneJob));         // status, done, finished, job
   b += (int64_t)sizeof(PackDesc) + 4;                      // descriptor, active-list entry
   return b;
@@ -117,7 +119,7 @@ int check_class(const gpb_slot_class& c) {
   if (c.max_bodies < 1 || c.max_bodies > GPB_MAX_BODIES || c.max_q < 0 || c.max_q > 7 * GPB_MAX_BODIES ||
       c.max_v < 0 || c.max_v > GPB_MAX_DOF || c.max_contacts < 0 || c.max_contacts > GPB_MAX_CONTACTS ||
       c.max_halfspaces < 0 || c.max_halfspaces > GPB_MAX_HALFSPACES || c.weight < 0.0 || c.packs < 0 ||
-      c.chunk_steps < 0)
+      c.chunk_steps < 0 || c.max_cuboids < 0 || c.max_cuboids > GPB_MAX_CUBOIDS)
     return fail(GPB_E_RANGE, "gpb_server: slot class capacity outside the documented limits");
   return GPB_OK;
 }
@@ -247,6 +249,7 @@ extern "C" int gpb_server_create(gpb_ctx* ctx, const gpb_server_opts* o, gpb_ser
       P.nv = C.caps.max_v;
       P.nc = C.caps.max_contacts;
       P.nh = C.caps.max_halfspaces;
+      P.nu = C.caps.max_cuboids;
       P.chain = 0;
       P.topo = rt;
       P.ctc = rc;
@@ -261,7 +264,7 @@ extern "C" int gpb_server_create(gpb_ctx* ctx, const gpb_server_opts* o, gpb_ser
       rq += P.nq;
       rv += P.nv;
       rl += LANE_I;
-      rs += scratch_layout(P.nb, P.nq, P.nv, P.nc).total;
+      rs += scratch_layout(P.nb, P.nq, P.nv, P.nc, P.nu).total;
       S->pack_class[p] = k;
     }
   }
@@ -388,7 +391,8 @@ extern "C" int gpb_server_submit(gpb_server* S, const gpb_model* m, int64_t firs
     for (int c = 0; c < (int)S->classes.size(); ++c) {
       const gpb_slot_class& cap = S->classes[c].caps;
       if (S->classes[c].npacks == 0 || R.info.nb > cap.max_bodies || R.info.nq > cap.max_q ||
-          R.info.nv > cap.max_v || R.info.nc > cap.max_contacts || R.info.nh > cap.max_halfspaces)
+          R.info.nv > cap.max_v || R.info.nc > cap.max_contacts || R.info.nh > cap.max_halfspaces ||
+          R.info.nu > cap.max_cuboids)
         continue;
       if (best < 0 || S->classes[c].pack_bytes < S->classes[best].pack_bytes) best = c;
     }
@@ -413,6 +417,10 @@ extern "C" int gpb_server_submit(gpb_server* S, const gpb_model* m, int64_t firs
       O.joint_armature.assign(m->joint_armature + I.j0, m->joint_armature + I.j0 + I.nb);
     else
       O.joint_armature.assign((size_t)I.nb, 0.0);
+    if (m->body_cuboid)
+      O.body_cuboid.assign(m->body_cuboid + 3 * (size_t)I.j0, m->body_cuboid + 3 * (size_t)(I.j0 + I.nb));
+    else
+      O.body_cuboid.assign(3 * (size_t)I.nb, 0.0);
     O.contact_offset = {0, I.nc};
     if (I.nc) {
       O.contact_body.assign(m->contact_body + I.c0, m->contact_body + I.c0 + I.nc);

@@ -14,7 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libgpb.so"
 # return codes / status bits / enums (include/gpb.h)
 GPB_OK = 0
 GPB_E_INVAL, GPB_E_NOMEM, GPB_E_CUDA, GPB_E_TIMEOUT, GPB_E_RANGE, GPB_E_STATE = -1, -2, -3, -4, -5, -6
-GPB_ST_NONFINITE, GPB_ST_CHOL_FAIL = 1, 2
+GPB_ST_NONFINITE, GPB_ST_CHOL_FAIL, GPB_ST_COLLISION = 1, 2, 4
 FIXED, REVOLUTE, PRISMATIC, FLOATING = 0, 1, 2, 3
 SEMI_IMPLICIT_EULER, RUNGE_KUTTA_2, RUNGE_KUTTA_4 = 0, 1, 2
 FP64, MIXED, MIXED_REFINED = 0, 1, 2
@@ -46,6 +46,7 @@ class GpbModel(C.Structure):
         ("halfspace_params", P_f64),
         ("contact_model", P_i32),
         ("joint_armature", P_f64),
+        ("body_cuboid", P_f64),
     ]
 
 
@@ -71,6 +72,7 @@ class GpbSlotClass(C.Structure):
         ("weight", C.c_double),
         ("packs", C.c_int32),
         ("chunk_steps", C.c_int32),
+        ("max_cuboids", C.c_int32),
     ]
 
 
@@ -144,6 +146,9 @@ SIGNATURES = [
     ("gpb_cvt_peak", C.c_int, [C.c_int, P_f64]),
     ("gpb_dynamics_static", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                       C.c_void_p, C.c_void_p]),
+    ("gpb_collide_cuboids", C.c_int, [C.c_void_p, C.c_int64, P_f64, P_f64, P_f64, P_f64, P_i32, P_f64, P_f64]),
+    ("gpb_collide_cuboids_device", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("gpb_server_plan", C.c_int, [C.POINTER(GpbServerOpts), P_i32, P_i64]),
     ("gpb_server_create", C.c_int, [C.c_void_p, C.POINTER(GpbServerOpts), C.POINTER(C.c_void_p)]),
     ("gpb_server_destroy", C.c_int, [C.c_void_p]),

@@ -8,7 +8,9 @@ reference can describe a mechanism the same way:
 * ``RevoluteJoint / PrismaticJoint / FloatingJoint / FixedJoint``
   (src/joint/*.rs; the transform maps the child frame to the parent frame)
 * ``SpatialInertia(frame, moment, cross_part, mass)`` (src/inertia.rs:31-37)
-* ``RigidBody(inertia)`` (src/rigid_body.rs:62-80), ``ContactPoint``
+* ``RigidBody(inertia)`` (src/rigid_body.rs:62-80) with
+  ``add_cuboid_collider(Cuboid.new_at_center(w, d, h))`` (src/rigid_body.rs:197-199),
+  ``ContactPoint``
   (src/contact.rs:16-38), ``HalfSpace`` (src/collision/halfspace.rs:6-36)
 * ``MechanismState(treejoints, bodies)`` (src/mechanism.rs:62-148): joint i's
   child must be body i and the parent is found by frame name, with the same
@@ -78,9 +80,31 @@ class HalfSpace:
 
 
 @dataclass
+class Cuboid:
+    """Cuboid collider centred on its body's frame (src/collision/cuboid.rs:7-15)."""
+    w: float
+    d: float
+    h: float
+
+    @staticmethod
+    def new_at_center(w: float, d: float, h: float) -> "Cuboid":
+        return Cuboid(float(w), float(d), float(h))
+
+    @staticmethod
+    def new_cube_at_center(l: float) -> "Cuboid":
+        return Cuboid(float(l), float(l), float(l))
+
+
+@dataclass
 class RigidBody:
     inertia: SpatialInertia
     contact_points: list = field(default_factory=list)
+    collider: Cuboid | None = None
+
+    def add_cuboid_collider(self, cuboid: Cuboid) -> None:
+        """RigidBody::add_cuboid_collider (src/rigid_body.rs:197-199).  The
+        collider's pose follows the body (src/mechanism.rs:257-275)."""
+        self.collider = cuboid
 
     def add_contact_point(self, cp: ContactPoint) -> None:
         if self.inertia.frame != cp.frame:
@@ -192,13 +216,17 @@ class Model:
 
     FIELDS = ("joint_offset", "joint_type", "joint_parent", "joint_iso", "joint_axis",
               "joint_spring", "body_inertia", "contact_offset", "contact_body", "contact_params",
-              "halfspace_offset", "halfspace_params", "contact_model", "joint_armature")
+              "halfspace_offset", "halfspace_params", "contact_model", "joint_armature",
+              "body_cuboid")
 
     def __init__(self, **arrays):
         i32 = ("joint_offset", "joint_type", "joint_parent", "contact_offset", "contact_body",
                "halfspace_offset", "contact_model")
+        nj = len(np.asarray(arrays["joint_type"]).ravel())
         if arrays.get("joint_armature") is None:  # optional: no armature
-            arrays["joint_armature"] = np.zeros(len(np.asarray(arrays["joint_type"]).ravel()))
+            arrays["joint_armature"] = np.zeros(nj)
+        if arrays.get("body_cuboid") is None:     # optional: no cuboid colliders
+            arrays["body_cuboid"] = np.zeros(3 * nj)
         for name in self.FIELDS:
             a = arrays[name]
             dt = np.int32 if name in i32 else np.float64
@@ -209,7 +237,7 @@ class Model:
     # -- construction -----------------------------------------------------
     @classmethod
     def from_mechanisms(cls, mechs: Sequence[MechanismState]) -> "Model":
-        jo, jt, jp, iso, ax, sp, inert, arm = [0], [], [], [], [], [], [], []
+        jo, jt, jp, iso, ax, sp, inert, arm, cub = [0], [], [], [], [], [], [], [], []
         co, cb, cp, ho, hp, cm = [0], [], [], [0], [], []
         for m in mechs:
             for j, b, p in zip(m.treejoints, m.bodies, m.parents):
@@ -219,6 +247,7 @@ class Model:
                 ax.extend(j.axis)
                 sp.extend(j.spring if j.spring is not None else (0.0, 0.0))
                 arm.append(j.armature)
+                cub.extend((b.collider.w, b.collider.d, b.collider.h) if b.collider else (0.0, 0.0, 0.0))
                 I = b.inertia
                 M = np.asarray(I.moment, float)
                 inert.extend([I.mass, *np.asarray(I.cross_part, float),
@@ -236,7 +265,7 @@ class Model:
         return cls(joint_offset=jo, joint_type=jt, joint_parent=jp, joint_iso=iso, joint_axis=ax,
                    joint_spring=sp, body_inertia=inert, contact_offset=co, contact_body=cb,
                    contact_params=cp, halfspace_offset=ho, halfspace_params=hp, contact_model=cm,
-                   joint_armature=arm)
+                   joint_armature=arm, body_cuboid=cub)
 
     @classmethod
     def from_config(cls, config: int, n: int, seed: int = 0,
@@ -309,6 +338,7 @@ class Model:
             parts["joint_axis"].append(self.joint_axis[3 * j0:3 * j1])
             parts["joint_spring"].append(self.joint_spring[2 * j0:2 * j1])
             parts["joint_armature"].append(self.joint_armature[j0:j1])
+            parts["body_cuboid"].append(self.body_cuboid[3 * j0:3 * j1])
             parts["body_inertia"].append(self.body_inertia[10 * j0:10 * j1])
             parts["contact_body"].append(self.contact_body[c0:c1])
             parts["contact_params"].append(self.contact_params[6 * c0:6 * c1])
@@ -327,7 +357,7 @@ class Model:
         out = {}
         for name in ("joint_type", "joint_parent", "joint_iso", "joint_axis", "joint_spring",
                      "body_inertia", "contact_body", "contact_params", "halfspace_params",
-                     "contact_model", "joint_armature"):
+                     "contact_model", "joint_armature", "body_cuboid"):
             out[name] = np.concatenate([getattr(m, name)[:cls._used(m, name)] for m in models])
         for name in ("joint_offset", "contact_offset", "halfspace_offset"):
             parts, base = [np.zeros(1, np.int64)], 0
@@ -343,7 +373,8 @@ class Model:
         """Length of the used part of a table (struct() may pad empty tables to one entry)."""
         nj, nc, nh = int(m.joint_offset[-1]), int(m.contact_offset[-1]), int(m.halfspace_offset[-1])
         per = {"joint_type": nj, "joint_parent": nj, "joint_iso": 7 * nj, "joint_axis": 3 * nj,
-               "joint_spring": 2 * nj, "joint_armature": nj, "body_inertia": 10 * nj, "contact_body": nc,
+               "joint_spring": 2 * nj, "joint_armature": nj, "body_cuboid": 3 * nj,
+               "body_inertia": 10 * nj, "contact_body": nc,
                "contact_params": 6 * nc, "halfspace_params": 8 * nh, "contact_model": m.n}
         return per[name]
 

@@ -31,11 +31,12 @@ class SlotClass:
     weight: float = 0.0  # share of hbm_budget_bytes (0: use `packs`)
     packs: int = 0       # packs of 32 slots
     chunk_steps: int = 0  # steps per tick of this class (0: the server's chunk_steps)
+    max_cuboids: int = 0  # cuboid colliders per instance
 
     def struct(self) -> _abi.GpbSlotClass:
         return _abi.GpbSlotClass(self.max_bodies, self.max_q, self.max_v, self.max_contacts,
                                  self.max_halfspaces, float(self.weight), int(self.packs),
-                                 int(self.chunk_steps))
+                                 int(self.chunk_steps), int(self.max_cuboids))
 
 
 # numpy image of gpb_request (same field order and alignment)

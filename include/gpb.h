@@ -56,6 +56,8 @@ extern "C" {
 #define GPB_ST_OK 0
 #define GPB_ST_NONFINITE 1 /* q, v, q̈ or a contact force became NaN/Inf   */
 #define GPB_ST_CHOL_FAIL 2 /* mass matrix not positive definite            */
+#define GPB_ST_COLLISION 4 /* cuboid GJK/EPA met a case the reference panics
+                              on, or ran past its loop / storage bounds   */
 
 /* ---- enums ------------------------------------------------------------ */
 /* Joint kinds of src/joint/mod.rs:21-27. */
@@ -136,6 +138,15 @@ enum gpb_control {
  *                   src/hybrid/articulated/mod.rs:244-247); NULL = none.  The
  *                   reference's continuous path has no such term, so leave it
  *                   NULL for parity with dynamics_continuous.
+ * body_cuboid[3j..] cuboid collider of body j centred on its frame and aligned
+ *                   with it (Cuboid::new_at_center(w, d, h) in
+ *                   RigidBody::add_cuboid_collider, src/rigid_body.rs:197-199;
+ *                   the pose follows the body, src/mechanism.rs:257-275):
+ *                   w, d, h along x, y, z; all zero (or NULL) = no collider.
+ *                   Every pair of cuboid bodies (i < j) is tested with GJK/EPA
+ *                   and pushed apart by the collider contact law
+ *                   (src/contact.rs:191-242,306-317).  At most GPB_MAX_CUBOIDS
+ *                   cuboids per instance.
  */
 typedef struct gpb_model {
   int64_t n_instances;
@@ -153,6 +164,7 @@ typedef struct gpb_model {
   const double* halfspace_params;
   const int32_t* contact_model;    /* [n_instances] */
   const double* joint_armature;    /* [n_joints] or NULL */
+  const double* body_cuboid;       /* [3 n_joints] or NULL */
 } gpb_model;
 
 /* Limits of one instance. */
@@ -160,6 +172,7 @@ typedef struct gpb_model {
 #define GPB_MAX_DOF 64
 #define GPB_MAX_CONTACTS 64
 #define GPB_MAX_HALFSPACES 4
+#define GPB_MAX_CUBOIDS 8
 
 /* ---- library / context ------------------------------------------------ */
 typedef struct gpb_ctx gpb_ctx;
@@ -227,6 +240,30 @@ int gpb_dynamics(gpb_batch* batch, const double* tau, int precision, double* qdd
 #define GPB_STATIC_SCRATCH_BYTES (16u << 20)
 int gpb_dynamics_static(gpb_batch* batch, const double* q, const double* v, const double* tau,
                         int precision, double* qdd, void* stream);
+
+/*
+ * CollisionDetector::new(A, B) followed by gjk() and epa()
+ * (src/collision/mod.rs:48-87; gjk.rs:14-125; epa.rs:108-254) for n
+ * independent pairs of cuboids, one GPU thread per pair.  pose_a / pose_b: 7
+ * doubles per pair (unit quaternion qx, qy, qz, qw, then the centre tx, ty,
+ * tz); size_a / size_b: (w, d, h) per pair.  result[i]: 1 = in collision, with
+ * cp_a / cp_b the contact points on A and on B (3 doubles each; cp_b − cp_a is
+ * the penetration, from A into B); 0 = no collision (cp = 0); -1 = a case where
+ * the reference panics (degenerate simplex, face or edge); -2 = the query ran
+ * past the kernel's storage bounds (more than 48 polytope vertices, 160
+ * faces, 32 horizon edges or 64 GJK iterations).  The decisions and the
+ * contact points are computed in the reference's order of operations with
+ * IEEE rounding.
+ * gpb_collide_cuboids takes host buffers and returns when the results are
+ * written.  gpb_collide_cuboids_device takes device buffers and only enqueues
+ * the kernel on `stream` (NULL = the context's stream).
+ */
+int gpb_collide_cuboids(gpb_ctx* ctx, int64_t n, const double* pose_a, const double* size_a,
+                        const double* pose_b, const double* size_b, int32_t* result, double* cp_a,
+                        double* cp_b);
+int gpb_collide_cuboids_device(gpb_ctx* ctx, int64_t n, const double* pose_a, const double* size_a,
+                               const double* pose_b, const double* size_b, int32_t* result,
+                               double* cp_a, double* cp_b, void* stream);
 
 /*
  * step (src/simulate.rs:20-83) for every instance: one integrator step of
@@ -382,6 +419,7 @@ typedef struct gpb_slot_class {
   double weight;  /* share of the budget left after the fixed classes; 0 = fixed */
   int32_t packs;  /* packs of 32 slots of a fixed class (weight 0) */
   int32_t chunk_steps; /* steps per tick of this class's requests (0 = the server's) */
+  int32_t max_cuboids; /* cuboid colliders per instance (0..GPB_MAX_CUBOIDS) */
 } gpb_slot_class;
 
 typedef struct gpb_server_opts {

@@ -19,6 +19,7 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 LIB = HERE / "liboracle.so"
 SRC = HERE / "gpb_oracle.cpp"
+SOURCES = (SRC, HERE / "collision.cpp")
 
 P_f64 = C.POINTER(C.c_double)
 P_i64 = C.POINTER(C.c_int64)
@@ -29,11 +30,11 @@ LU, CHOLESKY = 0, 1
 
 def build(force: bool = False) -> Path:
     """g++ -O2 -ffp-contract=off (x86 and Arm agree bit for bit)."""
-    if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime,
-                                                              (REPO / "include/gpb.h").stat().st_mtime):
+    deps = [*SOURCES, HERE / "collision.h", REPO / "include/gpb.h"]
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(p.stat().st_mtime for p in deps):
         tmp = LIB.with_suffix(".so.tmp")
         subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
-                        "-I", str(REPO / "include"), str(SRC), "-o", str(tmp), "-lpthread"],
+                        "-I", str(REPO / "include"), *map(str, SOURCES), "-o", str(tmp), "-lpthread"],
                        check=True)
         os.replace(tmp, LIB)
     return LIB
@@ -52,6 +53,8 @@ def lib():
         L.oracle_dynamics.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_int, P_f64, P_f64]
         L.oracle_mass_matrix.argtypes = [vp, C.c_int64, P_f64, P_f64]
         L.oracle_free_velocity.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_double, C.c_int, P_f64]
+        L.oracle_collide_cuboids.argtypes = [C.c_int64, P_f64, P_f64, P_f64, P_f64, C.c_int, P_i32,
+                                             P_f64, P_f64, P_i32]
         L.oracle_energy.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, P_f64]
         L.oracle_step.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_double, C.c_int, C.c_int]
         L.oracle_open_loop_tau.argtypes = [C.c_uint32, C.c_int64, C.c_int64, C.c_int32, C.c_double]
@@ -111,6 +114,24 @@ def free_velocity(model, i, q, v, tau=None, dt=1e-3, gravity=True):
     out = np.zeros(max(v.size, 1))
     st = lib().oracle_free_velocity(_m(model), i, _p(q), _p(v), _p(tau), dt, int(bool(gravity)), _p(out))
     return out[:v.size], st
+
+
+COL_HIT, COL_NONE = 1, 0
+
+
+def collide_cuboids(pose_a, dims_a, pose_b, dims_b, translate=True, stats=False):
+    """CollisionDetector::new(A, B).gjk() / .epa() (src/collision/mod.rs:48-87) for
+    n pairs: poses (n, 7) = (qx, qy, qz, qw, tx, ty, tz), dims (n, 3) = (w, d, h).
+    Returns (result codes (n,), cp_a (n, 3), cp_b (n, 3)[, stats (n, 6)])."""
+    f = lambda a, k: np.ascontiguousarray(np.asarray(a, float).reshape(-1, k))
+    pa, da, pb, db = f(pose_a, 7), f(dims_a, 3), f(pose_b, 7), f(dims_b, 3)
+    n = pa.shape[0]
+    res = np.zeros(n, np.int32)
+    ca, cb = np.zeros((n, 3)), np.zeros((n, 3))
+    stt = np.zeros((n, 6), np.int32)
+    lib().oracle_collide_cuboids(n, _p(pa), _p(da), _p(pb), _p(db), int(bool(translate)),
+                                 res.ctypes.data_as(P_i32), _p(ca), _p(cb), stt.ctypes.data_as(P_i32))
+    return (res, ca, cb, stt) if stats else (res, ca, cb)
 
 
 def mass_matrix(model, i, q):

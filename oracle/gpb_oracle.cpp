@@ -30,6 +30,7 @@
 #include <thread>
 #include <vector>
 
+#include "collision.h"
 #include "gpb.h"
 
 namespace orc {
@@ -236,6 +237,8 @@ struct Mechanism {
   std::vector<std::vector<int>> contact_ids;
   std::vector<HalfSpace> halfspaces;
   int contact_model;
+  std::vector<int> cuboid;          // per body: 1 = cuboid collider
+  std::vector<double> cuboid_dims;  // per body: w, d, h
   int nq, nv, ncontacts;
   std::vector<std::vector<int>> supports;  // supports[j] = bodies joint j+1 supports
 };
@@ -303,6 +306,16 @@ static bool load_mechanism(const gpb_model* m, int64_t inst, Mechanism& out) {
     out.halfspaces.push_back({{p[0], p[1], p[2]}, {p[3], p[4], p[5]}, p[6], p[7]});
   }
   out.contact_model = m->contact_model ? m->contact_model[inst] : GPB_HUNT_CROSSLEY;
+  // cuboid colliders (src/rigid_body.rs:197-199); all-zero sizes = none
+  out.cuboid.assign(nj, 0);
+  out.cuboid_dims.assign(3 * (size_t)nj, 0.0);
+  for (int a = 0; a < nj && m->body_cuboid; ++a) {
+    const double* d = m->body_cuboid + 3 * (size_t)(j0 + a);
+    if (d[0] == 0.0 && d[1] == 0.0 && d[2] == 0.0) continue;
+    if (!(d[0] > 0.0 && d[1] > 0.0 && d[2] > 0.0)) return false;
+    out.cuboid[a] = 1;
+    for (int e = 0; e < 3; ++e) out.cuboid_dims[3 * (size_t)a + e] = d[e];
+  }
   // supports (src/mechanism.rs:118-125)
   out.supports.assign(nj, {});
   for (int a = 0; a < nj; ++a) {
@@ -383,25 +396,9 @@ static void jacobian_transform(SV* cols, int n, const Iso& x) {
   }
 }
 
-// calculate_contact_force (src/contact.rs:260-302) with the halfspace constants
-// (src/contact.rs:321-338).  The LINEAR_SPRING_DAMPER law replaces only the
-// normal-force line.
-static V3 contact_force(int model, double penetration, V3 normal, V3 velocity, double k_point,
-                        double damping, double alpha, double mu) {
-  double z = penetration;
-  double z_dot = -dot(velocity, normal);
-  double pi;
-  if (model == GPB_LINEAR_SPRING_DAMPER) {
-    pi = std::fmax(k_point * z + damping * z_dot, 0.0);
-  } else {
-    double zn = std::pow(z, 1.5);
-    double k_h = 50e3;
-    double k = k_point * k_h / (k_point + k_h);
-    double lambda = 3.0 / 2.0 * alpha * k;
-    // Rust f64::max returns the non-NaN operand: a NaN z^1.5 (z < 0 within
-    // the margin) gives 0, which std::fmax also does.
-    pi = std::fmax(lambda * zn * z_dot + k * zn, 0.0);
-  }
+// The normal force π n plus the regularised Coulomb friction of
+// calculate_contact_force (src/contact.rs:260-302).
+static V3 friction_force(double pi, V3 normal, V3 velocity, double z_dot, double mu) {
   V3 f_normal = normal * pi;
   V3 v_t = velocity + normal * z_dot;
   double v_t_norm = norm(v_t);
@@ -415,6 +412,41 @@ static V3 contact_force(int model, double penetration, V3 normal, V3 velocity, d
     f_fric = dir * (-mu_e * pi);
   }
   return f_normal + f_fric;
+}
+
+// calculate_contact_force (src/contact.rs:260-302): Hunt–Crossley normal force
+// with k = k_a k_b / (k_a + k_b), λ = 1.5 α k.
+static V3 hunt_crossley(double z, V3 normal, V3 velocity, double k_a, double k_b, double alpha,
+                        double mu) {
+  double z_dot = -dot(velocity, normal);
+  double zn = std::pow(z, 1.5);
+  double k = k_a * k_b / (k_a + k_b);
+  double lambda = 3.0 / 2.0 * alpha * k;
+  // Rust f64::max returns the non-NaN operand: a NaN z^1.5 (z < 0 within
+  // the margin) gives 0, which std::fmax also does.
+  double pi = std::fmax(lambda * zn * z_dot + k * zn, 0.0);
+  return friction_force(pi, normal, velocity, z_dot, mu);
+}
+
+// Point / sphere against a half-space (src/contact.rs:321-338: k_h = 50e3).
+// The LINEAR_SPRING_DAMPER law replaces only the normal-force line.
+static V3 contact_force(int model, double penetration, V3 normal, V3 velocity, double k_point,
+                        double damping, double alpha, double mu) {
+  if (model != GPB_LINEAR_SPRING_DAMPER)
+    return hunt_crossley(penetration, normal, velocity, k_point, 50e3, alpha, mu);
+  double z_dot = -dot(velocity, normal);
+  double pi = std::fmax(k_point * penetration + damping * z_dot, 0.0);
+  return friction_force(pi, normal, velocity, z_dot, mu);
+}
+
+// calculate_contact_force_collider (src/contact.rs:306-317): the force from B
+// on A, k = 5e3 for both shapes, α = 1, μ = 1.  A zero-depth contact gives a
+// NaN normal, as UnitVector3::new_normalize of a zero vector does.
+static V3 collider_force(V3 cp_a, V3 cp_b, V3 velocity) {
+  V3 pen = cp_b - cp_a;
+  double n = norm(pen);
+  V3 normal{pen.x / n, pen.y / n, pen.z / n};
+  return hunt_crossley(n, normal, velocity, 5e3, 5e3, 1.0, 1.0);
 }
 
 struct Work {
@@ -488,8 +520,11 @@ static void mass_matrix(const Mechanism& M, const std::vector<Iso>& X, std::vect
     for (int j = i + 1; j < nv; ++j) H[(size_t)i * nv + j] = lower[(size_t)j * nv + i];
 }
 
-// contact_dynamics, point-vs-halfspace part (src/contact.rs:97-128,188).
-static void contact_dynamics(const Mechanism& M, const std::vector<Iso>& X,
+// contact_dynamics (src/contact.rs:97-245): point / sphere contacts against the
+// half-spaces, then every pair of cuboid colliders (GJK + EPA in the frame
+// translated to the first cuboid, as CollisionDetector does).  Returns 0, or
+// GPB_ST_COLLISION where the reference would panic.
+static int contact_dynamics(const Mechanism& M, const std::vector<Iso>& X,
                              const std::vector<SV>& T, std::vector<SV>& W, double* force_out) {
   int n = (int)M.joints.size();
   W.assign(n + 1, SV{{0, 0, 0}, {0, 0, 0}});
@@ -531,6 +566,37 @@ static void contact_dynamics(const Mechanism& M, const std::vector<Iso>& X,
     }
     W[a + 1] = wr;
   }
+  // cuboid pairs (src/contact.rs:191-242); collider poses are the bodies'
+  // poses (MechanismState::update_collider_poses, src/mechanism.rs:257-275)
+  for (int a = 0; a < n; ++a) {
+    if (!M.cuboid[a]) continue;
+    for (int b = a + 1; b < n; ++b) {
+      if (!M.cuboid[b]) continue;
+      const M3 Ra = to_rotation_matrix(X[a + 1].r), Rb = to_rotation_matrix(X[b + 1].r);
+      double ra[9], rb[9];
+      for (int e = 0; e < 9; ++e) {
+        ra[e] = Ra.m[e / 3][e % 3];
+        rb[e] = Rb.m[e / 3][e % 3];
+      }
+      const double ta[3] = {X[a + 1].t.x, X[a + 1].t.y, X[a + 1].t.z};
+      const double tb[3] = {X[b + 1].t.x, X[b + 1].t.y, X[b + 1].t.z};
+      double ca[3], cb[3];
+      const int r = orc_col::collide(ra, ta, &M.cuboid_dims[3 * (size_t)a], rb, tb, &M.cuboid_dims[3 * (size_t)b],
+                                     true, ca, cb, nullptr);
+      if (r < 0) return GPB_ST_COLLISION;
+      if (r != orc_col::COL_HIT) continue;
+      const V3 cpa{ca[0], ca[1], ca[2]}, cpb{cb[0], cb[1], cb[2]};
+      const V3 va = T[a + 1].lin + cross(T[a + 1].ang, cpa);  // Twist::point_velocity
+      const V3 vb = T[b + 1].lin + cross(T[b + 1].ang, cpb);
+      const V3 f = collider_force(cpa, cpb, va - vb);
+      W[a + 1].ang = W[a + 1].ang + cross(cpa, f);  // Wrench::from_force
+      W[a + 1].lin = W[a + 1].lin + f;
+      const V3 fn = -f;
+      W[b + 1].ang = W[b + 1].ang + cross(cpb, fn);
+      W[b + 1].lin = W[b + 1].lin + fn;
+    }
+  }
+  return 0;
 }
 
 // dynamics_bias (src/dynamics.rs:233-251) with bias_accelerations (200-224),
@@ -650,7 +716,8 @@ static bool chol_solve(std::vector<double> A, int n, std::vector<double>& b) {
 }
 
 // dynamics_continuous (src/dynamics.rs:322-364).  solver 0 = LU (reference),
-// 1 = Cholesky.  Returns 0, or GPB_ST_CHOL_FAIL if the solve failed.
+// 1 = Cholesky.  Returns 0, GPB_ST_CHOL_FAIL if the solve failed, or
+// GPB_ST_COLLISION if the cuboid collision met a case the reference panics on.
 static int dynamics(const Mechanism& M, const double* q, const double* v, const double* tau,
                     int solver, double* qdd, double* cforce, Work& w) {
   int n = (int)M.joints.size();
@@ -660,7 +727,8 @@ static int dynamics(const Mechanism& M, const double* q, const double* v, const 
   w.T.assign(n + 1, SV{{0, 0, 0}, {0, 0, 0}});
   for (int a = 0; a < n; ++a) w.T[a + 1] = sv_add(w.T[M.joints[a].parent], twist_transform(w.jt[a], w.X[a + 1]));
   mass_matrix(M, w.X, w.M);
-  contact_dynamics(M, w.X, w.T, w.Wc, cforce);
+  const int cst = contact_dynamics(M, w.X, w.T, w.Wc, cforce);
+  if (cst) return cst;
   dynamics_bias(M, w.X, w.jt, w.T, w.Wc, w.c);
   std::vector<double> rhs(M.nv);
   for (int i = 0; i < M.nv; ++i) rhs[i] = tau ? tau[i] : 0.0;
@@ -889,6 +957,31 @@ int oracle_dynamics(const gpb_model* m, int64_t inst, const double* q, const dou
   if (!orc::load_mechanism(m, inst, M)) return GPB_E_INVAL;
   orc::Work w;
   return orc::dynamics(M, q, v, tau, solver, qdd, contact_force, w);
+}
+
+// CollisionDetector::new(A, B) then gjk() and epa() (src/collision/mod.rs:48-87)
+// for n pairs of cuboids: pose = (qx, qy, qz, qw, tx, ty, tz), dims = (w, d, h).
+// translate = 0 runs gjk / epa on the shapes where they are (the reference's
+// gjk / epa unit tests).  result[i] = orc_col outcome code; cp_a / cp_b are
+// written for hits; stats (6 ints per pair: GJK iterations, EPA expansions,
+// vertices, triangles, edges, heap size) may be NULL.
+int oracle_collide_cuboids(int64_t n, const double* pose_a, const double* dims_a, const double* pose_b,
+                           const double* dims_b, int translate, int32_t* result, double* cp_a, double* cp_b,
+                           int32_t* stats) {
+  for (int64_t i = 0; i < n; ++i) {
+    double ra[9], rb[9];
+    orc_col::quat_to_matrix(pose_a + 7 * i, ra);
+    orc_col::quat_to_matrix(pose_b + 7 * i, rb);
+    orc_col::Stats st;
+    for (int e = 0; e < 3; ++e) cp_a[3 * i + e] = cp_b[3 * i + e] = 0.0;
+    result[i] = orc_col::collide(ra, pose_a + 7 * i + 4, dims_a + 3 * i, rb, pose_b + 7 * i + 4, dims_b + 3 * i,
+                                 translate != 0, cp_a + 3 * i, cp_b + 3 * i, &st);
+    if (stats) {
+      const int32_t v[6] = {st.gjk_iters, st.epa_iters, st.verts, st.tris, st.edges, st.heap};
+      for (int e = 0; e < 6; ++e) stats[6 * i + e] = v[e];
+    }
+  }
+  return 0;
 }
 
 // Articulated::free_velocity (src/hybrid/articulated/mod.rs:124-199,
