@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--serve-precisions", default="mixed,fp64")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM budget of the slot pool")
     ap.add_argument("--serve-algorithm", default="aba", choices=["aba", "crba"])
+    ap.add_argument("--cuboids", action="store_true",
+                    help="cuboid-collider workload: build_gripper batches (GJK/EPA jaw-cube "
+                         "contacts) and independent collision queries")
+    ap.add_argument("--pairs", type=int, default=1 << 22, help="collision queries per timed launch")
     return ap.parse_args()
 
 
@@ -215,6 +219,28 @@ def run_reference(args):
                                    f"restatement of the reference path (Rust crate unbuildable here)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    print(json.dumps(line))
+    return 0
+
+
+def run_reference_cuboids(args):
+    """--cuboids --impl reference: the oracle on the gripper workload, rank 0 only."""
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+
+    oracle.build()
+    M, q0, v0 = gripper_batch(args.instances, args.seed)
+    base = cpu_cuboids(M, q0, v0, args.steps)
+    line = {"metric": "instance-steps/s of build_gripper batches (GJK/EPA cuboid contacts)",
+            "value": base["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy draws)", "impl": "reference",
+            "config": {"workload": f"gripper x {args.instances}", "dt": CUBOID_DT,
+                       "integrator": "semi-implicit Euler"},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
@@ -589,12 +615,202 @@ def run_serve(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# cuboid colliders: build_gripper batches (both jaws 0.02-0.07 m into the cube,
+# every evaluation runs 3 GJK/EPA pair queries per instance) and independent
+# collision queries (gpb_collide_cuboids_device)
+
+CUBOID_DT = 1e-5  # the squeezed 0.1 kg cube's regularised friction needs it
+
+
+def gripper_batch(n, seed):
+    from gpb import Model, builders
+
+    M = Model.from_mechanisms([builders.build_gripper()] * n)
+    q, v = builders.gripper_states(np.random.default_rng(seed), n)
+    return M, q.ravel(), v.ravel()
+
+
+def run_cuboids(args):
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import ctypes
+
+    import gpb
+    from gpb import Batch, builders
+    from gpb.flops import aba_model_flops, model_flops
+
+    L = gpb.lib()
+    ctx = gpb.Context(local)
+    n = args.instances
+    M, q0, v0 = gripper_batch(n, shard_seed(args.seed, rank))
+    B = Batch(M, ctx)
+    work = json.loads((ROOT / "profiles" / "collision_work.json").read_text())
+    pair_flops = work["gripper"]["mean_flops_per_evaluation"]
+    MODES = {"fp64": (gpb.FP64, gpb.ALGO_ABA, aba_model_flops(M, False)),
+             "fp64_crba": (gpb.FP64, gpb.ALGO_CRBA, model_flops(M, 0)),
+             "mixed": (gpb.MIXED, gpb.ALGO_ABA, aba_model_flops(M, True))}
+
+    def peak():
+        t = ctypes.c_double()
+        gpb._abi.check(L.gpb_fma_peak(local, gpb.FP64, 32, ctypes.byref(t)), "gpb_fma_peak")
+        return t.value
+
+    p64 = peak()
+    results = {}
+    for name, (prec, algo, inst_flops) in MODES.items():
+        B.set_algorithm(algo)
+        B.update(q0, v0)
+        B.clear_status()
+        w, _ = B.autotune(CUBOID_DT, 0, prec, trial_steps=10)
+        if args.warmup:
+            B.simulate_steps(args.warmup, CUBOID_DT, 0, prec)
+        if world > 1:
+            torch.distributed.barrier()
+        ctx.synchronize()
+        with Clocks(local) as clk:
+            l0 = ctx.launches
+            B.simulate_steps(args.steps, CUBOID_DT, 0, prec, step0=args.warmup)
+            kernel_ms = L.gpb_last_launch_ms(ctx.h)
+            ctx.synchronize()
+            launches = ctx.launches - l0
+        kernel_ms = all_reduce(kernel_ms, "max", world, f"cuda:{local}")
+        done = B.steps_done()
+        flops = float(np.dot(done, inst_flops.astype(np.float64))) + float(done.sum()) * pair_flops
+        results[name] = {"kernel_ms": kernel_ms, "clocks": clk.summary(), "launches": launches,
+                         "warps_per_sm": w, "failed_instances": int(np.sum(B.status() != 0)),
+                         "done": all_reduce(float(done.sum()), "sum", world, f"cuda:{local}"),
+                         "flops": all_reduce(flops, "sum", world, f"cuda:{local}")}
+    head_name = max(("fp64", "fp64_crba"), key=lambda k: results[k]["done"] / results[k]["kernel_ms"])
+    head = results[head_name]
+
+    def roof(r, extra):
+        ach = r["flops"] / (r["kernel_ms"] * 1e-3) / 1e12
+        return {"bound": "fp64", "achieved": ach, "peak": p64, "unit": "TFLOP/s", "frac": ach / p64,
+                "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (gpb_fma_peak), this run",
+                "work": extra}
+
+    # independent collision queries on device buffers, CUDA events on the stream
+    # the kernel runs on
+    queries = {}
+    stream = torch.cuda.Stream()  # a stream of its own: events and kernel on the same one
+    for kind in ("shallow", "deep"):
+        rng = np.random.default_rng(shard_seed(args.seed, rank))
+        pa, da, pb, db = builders.cuboid_pairs(rng, args.pairs, kind)
+        dev = {k: torch.from_numpy(np.ascontiguousarray(x)).cuda() for k, x in
+               (("pa", pa), ("da", da), ("pb", pb), ("db", db))}
+        res = torch.empty(args.pairs, dtype=torch.int32, device="cuda")
+        ca = torch.empty((args.pairs, 3), dtype=torch.float64, device="cuda")
+        cb = torch.empty_like(ca)
+
+        def launch():
+            gpb.collision.collide_cuboids_device(ctx, args.pairs, dev["pa"].data_ptr(), dev["da"].data_ptr(),
+                                                 dev["pb"].data_ptr(), dev["db"].data_ptr(), res.data_ptr(),
+                                                 ca.data_ptr(), cb.data_ptr(), stream.cuda_stream)
+
+        torch.cuda.synchronize()
+        for _ in range(3):
+            launch()
+        torch.cuda.synchronize()
+        reps = 10
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = ctx.launches
+        with Clocks(local) as clk:
+            e0.record(stream)
+            for _ in range(reps):
+                launch()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        assert ctx.launches - l0 == reps
+        per = work["pairs_" + kind]["mean_flops"]
+        ach = args.pairs * per / (ms * 1e-3) / 1e12
+        queries[kind] = {"pairs_per_s": args.pairs / (ms * 1e-3), "ms_per_launch": ms, "launches": reps,
+                         "hit_fraction": float((res == 1).float().mean()),
+                         "failed": int((res < 0).sum()), "clocks": clk.summary(),
+                         "roofline": {"bound": "fp64", "achieved": ach, "peak": p64, "unit": "TFLOP/s",
+                                      "frac": ach / p64, "traffic": None,
+                                      "work": f"{per:.0f} FP64 operations per query (mean, "
+                                              f"profiles/collision_work.json: {work['pairs_' + kind]['sample']})"}}
+        del dev, res, ca, cb
+    # e2e through the public API: pinned host state in, K steps, state out
+    q_h = torch.from_numpy(q0).pin_memory().numpy()
+    v_h = torch.from_numpy(v0).pin_memory().numpy()
+    prec, algo, _ = MODES[head_name]
+    B.set_algorithm(algo)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    B.update(q_h, v_h)
+    B.simulate_steps(args.steps, CUBOID_DT, 0, prec)
+    qo, vo = B.state()
+    e2e_s = all_reduce(time.perf_counter() - t0, "max", world, f"cuda:{local}")
+    e2e_done = all_reduce(float(B.steps_done().sum()), "sum", world, f"cuda:{local}")
+    line = {
+        "metric": "instance-steps/s of build_gripper batches (GJK/EPA cuboid contacts)",
+        "value": head["done"] / (head["kernel_ms"] * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["kernel_ms"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded numpy draws of gripper states and cuboid pairs)",
+        "config": {"workload": f"gripper x {n} per GPU (3 cuboid pairs per evaluation)",
+                   "algorithm": {"fp64": "articulated-body algorithm",
+                                 "fp64_crba": "CRBA + Cholesky (the reference's route)"}[head_name],
+                   "dt": CUBOID_DT, "integrator": "semi-implicit Euler", "control": "host (zero torque)",
+                   "l2": "inputs larger than L2 (topology + state + scratch > 129 MB)"},
+        "gpu_launches": head["launches"],
+        "roofline": roof(head, f"{pair_flops:.0f} FP64 operations of the 3 pair queries per evaluation "
+                               f"(profiles/collision_work.json) + the dynamics flops (gpb.flops)"),
+        "clocks": head["clocks"],
+        "modes": {k: {"value": r["done"] / (r["kernel_ms"] * 1e-3), "ms_per_step": r["kernel_ms"] / args.steps,
+                      "warps_per_sm": r["warps_per_sm"], "failed_instances": r["failed_instances"],
+                      "roofline": roof(r, "as above")} for k, r in results.items()},
+        "collision_queries": {"n_pairs": args.pairs, **queries},
+        "e2e": {"value": e2e_done / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (q_h.nbytes + v_h.nbytes) / args.steps,
+                "d2h_bytes_per_step": (qo.nbytes + vo.nbytes) / args.steps,
+                "note": "gpb_set_state (pinned host) + gpb_simulate + gpb_get_state"},
+    }
+    if rank == 0 and not args.skip_cpu:
+        line["cpu_baseline"] = cpu_cuboids(M, q0, v0, args.steps)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def cpu_cuboids(M, q0, v0, steps, seconds_target=12.0):
+    """The oracle on a bounded sample of the gripper batch, all host threads."""
+    import oracle
+
+    threads = os.cpu_count() or 1
+    q, v = q0.copy(), v0.copy()
+    cal = min(M.n, 8 * threads)
+    t = time.perf_counter()
+    oracle.simulate_batch(M, q, v, CUBOID_DT, 2, end=cal, threads=threads)
+    per = (time.perf_counter() - t) / (cal * 2)
+    sample = min(M.n, 4096)
+    K = max(5, min(steps, int(seconds_target / max(per * sample, 1e-9))))
+    q, v = q0.copy(), v0.copy()
+    t = time.perf_counter()
+    oracle.simulate_batch(M, q, v, CUBOID_DT, K, end=sample, threads=threads)
+    el = time.perf_counter() - t
+    return {"value": sample * K / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {sample} of {M.n} grippers x {K} steps (oracle restatement, {threads} host threads)"}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
-        return run_reference(args)
+        return run_reference_cuboids(args) if args.cuboids else run_reference(args)
     if args.serve:
         return run_serve(args)
+    if args.cuboids:
+        return run_cuboids(args)
     return run_gpu(args)
 
 

@@ -16,6 +16,10 @@
 // scan walks the heap in storage order, and that order fixes the numbering
 // of new faces and so how later ties between equal distances break.
 //
+// Values the reference recomputes (a face's |w| and w·w, tests of |x| == 0)
+// are computed once here, by the same operations, or tested as x·x == 0
+// (equivalent under IEEE rounding, NaN included): the results are unchanged.
+//
 // Storage is fixed per lane (local memory): MAXV polytope vertices, MAXT
 // faces ever created, MAXE horizon edges, GJK_MAX support evaluations.  Over
 // 4·10⁵ random pairs (shallow face contacts and deep random overlaps) the
@@ -132,9 +136,9 @@ __device__ __forceinline__ int gjk(const Shapes& S, D3 cA, D3 cB, PV* s) {
       const D3 v1 = s[0].v, v2 = s[1].v;
       const D3 v1v2 = sub(v2, v1);
       dir = cross(cross(v1, v2), v1v2);
-      if (norm(dir) == 0.0) {  // origin on the edge
+      if (norm2(dir) == 0.0) {  // origin on the edge (|x| == 0 ⟺ x·x == 0, NaN in both)
         const D3 cand = cross(v1v2, D3{1.0, 0.0, 0.0});
-        dir = norm(cand) > 0.0 ? cand : cross(v1v2, D3{0.0, 1.0, 0.0});
+        dir = norm2(cand) > 0.0 ? cand : cross(v1v2, D3{0.0, 1.0, 0.0});
       }
     } else if (n == 3) {
       const D3 v1 = s[0].v, v2 = s[1].v, v3 = s[2].v;
@@ -145,7 +149,7 @@ __device__ __forceinline__ int gjk(const Shapes& S, D3 cA, D3 cB, PV* s) {
         s[1] = s[2];
         s[2] = t;
       }
-      if (norm(dir) == 0.0) return CG_PANIC;  // colinear simplex
+      if (norm2(dir) == 0.0) return CG_PANIC;  // colinear simplex
     } else {
       const PV p1 = s[0], p2 = s[1], p3 = s[2], p4 = s[3];
       const D3 v1 = p1.v, v2 = p2.v, v3 = p3.v, v4 = p4.v;
@@ -209,7 +213,8 @@ __device__ __forceinline__ D3 closest_area(D3 v1, D3 v2, D3 v3) {
 struct Poly {
   double vx[MAXV], vy[MAXV], vz[MAXV];
   uint8_t via[MAXV], vib[MAXV];
-  double wx[MAXT], wy[MAXT], wz[MAXT], dist[MAXT];
+  double wx[MAXT], wy[MAXT], wz[MAXT];
+  double dist[MAXT], wn2[MAXT];  // |w| (the heap key) and w·w, computed once per face
   uint8_t t0[MAXT], t1[MAXT], t2[MAXT], obs[MAXT];
   uint16_t heap[MAXT];
   uint8_t e0[MAXE], e1[MAXE];
@@ -293,7 +298,8 @@ struct Poly {
     wx[nt] = w.x;
     wy[nt] = w.y;
     wz[nt] = w.z;
-    dist[nt] = norm(w);
+    wn2[nt] = norm2(w);
+    dist[nt] = __dsqrt_rn(wn2[nt]);  // = norm(w)
     push(nt);
     ++nt;
     return true;
@@ -324,15 +330,15 @@ __device__ __forceinline__ int epa(const Shapes& S, const PV* s, Poly& P, D3* cp
     const D3 w = P.w(index);
     const D3 v1 = P.v(i1), v2 = P.v(i2), v3 = P.v(i3);
     const D3 normal = cross(sub(v2, v1), sub(v3, v1));
-    if (norm(normal) == 0.0) return CG_PANIC;
+    if (norm2(normal) == 0.0) return CG_PANIC;
     const D3 direction = normal;
     const PV v = support_fn(S, direction);
     const double v_dot_w = dot(v.v, w);
-    const double wn2 = norm2(w);
+    const double wn2 = P.wn2[index], wn = P.dist[index];
     if (v_dot_w < sb_(wn2, 1e-8)) return CG_PANIC;  // below the face
-    if (dot(v.v, direction) < 0.0) return CG_PANIC;
-    if (dv_(sb_(v_dot_w, wn2), norm(w)) < 1e-6 ||
-        (norm(w) == 0.0 && dv_(dot(v.v, direction), norm(direction)) < 1e-6)) {
+    const double v_dot_d = dot(v.v, direction);
+    if (v_dot_d < 0.0) return CG_PANIC;
+    if (dv_(sb_(v_dot_w, wn2), wn) < 1e-6 || (wn == 0.0 && dv_(v_dot_d, norm(direction)) < 1e-6)) {
       double l[3];
       D3 n;
       lambda_area(v1, v2, v3, l, &n);
@@ -351,11 +357,11 @@ __device__ __forceinline__ int epa(const Shapes& S, const PV* s, Poly& P, D3* cp
     for (int h = 0; h < P.nh; ++h) {
       const int i = P.heap[h];
       if (P.obs[i]) continue;
-      const D3 wi = P.w(i);
+      const double wni = P.dist[i];
       bool seen = false;
-      if (norm(wi) != 0.0 && dot(v.v, wi) > ad_(norm2(wi), 0.0)) {
+      if (wni != 0.0 && dot(v.v, P.w(i)) > ad_(P.wn2[i], 0.0)) {
         seen = true;
-      } else if (!(norm(wi) > 0.0)) {  // a face through the origin, seen along its normal
+      } else if (!(wni > 0.0)) {  // a face through the origin, seen along its normal
         const D3 a = P.v(P.t0[i]);
         const D3 tn = cross(sub(P.v(P.t1[i]), a), sub(P.v(P.t2[i]), a));
         seen = dot(v.v, tn) > 0.0;
@@ -375,7 +381,7 @@ __device__ __forceinline__ int epa(const Shapes& S, const PV* s, Poly& P, D3* cp
       const int a = P.e0[k], b = P.e1[k];
       const D3 ea = P.v(a), eb = P.v(b);
       const D3 tn = cross(sub(eb, ea), sub(v.v, ea));
-      if (norm(tn) == 0.0) return CG_PANIC;
+      if (norm2(tn) == 0.0) return CG_PANIC;
       if (dot(tn, ea) < 0.0) return CG_PANIC;
       if (!P.add_face(a, b, vi)) return CG_OVERFLOW;
     }

@@ -122,13 +122,14 @@ COL_HIT, COL_NONE = 1, 0
 def collide_cuboids(pose_a, dims_a, pose_b, dims_b, translate=True, stats=False):
     """CollisionDetector::new(A, B).gjk() / .epa() (src/collision/mod.rs:48-87) for
     n pairs: poses (n, 7) = (qx, qy, qz, qw, tx, ty, tz), dims (n, 3) = (w, d, h).
-    Returns (result codes (n,), cp_a (n, 3), cp_b (n, 3)[, stats (n, 6)])."""
+    Returns (result codes (n,), cp_a (n, 3), cp_b (n, 3)[, stats (n, 7): GJK
+    iterations, EPA expansions, vertices, faces, edges, heap size, FP64 operations])."""
     f = lambda a, k: np.ascontiguousarray(np.asarray(a, float).reshape(-1, k))
     pa, da, pb, db = f(pose_a, 7), f(dims_a, 3), f(pose_b, 7), f(dims_b, 3)
     n = pa.shape[0]
     res = np.zeros(n, np.int32)
     ca, cb = np.zeros((n, 3)), np.zeros((n, 3))
-    stt = np.zeros((n, 6), np.int32)
+    stt = np.zeros((n, 7), np.int32)
     lib().oracle_collide_cuboids(n, _p(pa), _p(da), _p(pb), _p(db), int(bool(translate)),
                                  res.ctypes.data_as(P_i32), _p(ca), _p(cb), stt.ctypes.data_as(P_i32))
     return (res, ca, cb, stt) if stats else (res, ca, cb)

@@ -38,17 +38,42 @@
 namespace orc_col {
 namespace {
 
+// Operation count of the current query (the algorithmic work the throughput
+// figures are measured against): add, sub, mul, div and sqrt count 1 each.
+thread_local long long g_flops = 0;
+
 struct V {
   double x, y, z;
 };
-inline V add(V a, V b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-inline V sub(V a, V b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V add(V a, V b) {
+  g_flops += 3;
+  return {a.x + b.x, a.y + b.y, a.z + b.z};
+}
+inline V sub(V a, V b) {
+  g_flops += 3;
+  return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
 inline V neg(V a) { return {-a.x, -a.y, -a.z}; }
-inline V scale(double s, V a) { return {s * a.x, s * a.y, s * a.z}; }
-inline double dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-inline V cross(V a, V b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-inline double norm2(V a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
-inline double norm(V a) { return std::sqrt(norm2(a)); }
+inline V scale(double s, V a) {
+  g_flops += 3;
+  return {s * a.x, s * a.y, s * a.z};
+}
+inline double dot(V a, V b) {
+  g_flops += 5;
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+inline V cross(V a, V b) {
+  g_flops += 9;
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline double norm2(V a) {
+  g_flops += 5;
+  return a.x * a.x + a.y * a.y + a.z * a.z;
+}
+inline double norm(V a) {
+  g_flops += 1;
+  return std::sqrt(norm2(a));
+}
 inline bool is_zero(V a) { return a.x == 0.0 && a.y == 0.0 && a.z == 0.0; }
 
 // Cuboid corner points in world (or detector) coordinates, in the order of
@@ -59,6 +84,7 @@ struct Box {
 Box make_box(const double* R, V t, const double* dims) {
   Box b;
   const double hw = dims[0] / 2.0, hd = dims[1] / 2.0, hh = dims[2] / 2.0;
+  g_flops += 3 + 8 * 15;  // half sizes; R c per corner (+ t counted by add)
   for (int k = 0; k < 8; ++k) {
     const V c{(k & 1) ? -hw : hw, (k & 2) ? -hd : hd, (k & 4) ? -hh : hh};
     const V r{R[0] * c.x + R[1] * c.y + R[2] * c.z, R[3] * c.x + R[4] * c.y + R[5] * c.z,
@@ -165,6 +191,7 @@ void lambda_area(V v1, V v2, V v3, double* lam, V* normal) {
   const double inv = 1.0 / norm2(n);
   const double b3 = dot(cross(v1, v1v2), n) * inv;
   const double b2 = dot(cross(v1v3, v1), n) * inv;
+  g_flops += 5;
   lam[0] = 1.0 - (b2 + b3);
   lam[1] = b2;
   lam[2] = b3;
@@ -176,6 +203,7 @@ V closest_area(V v1, V v2, V v3) {
   lambda_area(v1, v2, v3, l, &n);
   const V w = add(add(scale(l[0], v1), scale(l[1], v2)), scale(l[2], v3));
   const double s = dot(w, n), nn = norm2(n);
+  g_flops += 6;
   return {s * n.x / nn, s * n.y / nn, s * n.z / nn};
 }
 
@@ -290,6 +318,7 @@ int epa(const std::vector<PV>& simplex, const Box& A, const Box& B, V* cpA, V* c
     const PV v = support_fn(A, B, direction);
     const double v_dot_w = dot(v.v, w);
     const double wn2 = norm2(w);
+    g_flops += 4;  // the three explicit operations of the tests below (and a division)
     if (v_dot_w < wn2 - 1e-8) return COL_EPA_BELOW;
     if (dot(v.v, direction) < 0.0) return COL_EPA_OPPOSITE;
     if ((v_dot_w - wn2) / norm(w) < 1e-6 ||
@@ -364,6 +393,7 @@ void quat_to_matrix(const double* q, double* R) {
 
 int collide(const double* RA, const double* tA, const double* dA, const double* RB, const double* tB,
             const double* dB, bool translate, double* cp_a, double* cp_b, Stats* st) {
+  g_flops = 0;
   V ta{tA[0], tA[1], tA[2]}, tb{tB[0], tB[1], tB[2]};
   const V off = ta;
   if (translate) {  // Isometry3::append_translation_mut(−t_A) on both shapes
@@ -373,14 +403,17 @@ int collide(const double* RA, const double* tA, const double* dA, const double* 
   const Box A = make_box(RA, ta, dA), B = make_box(RB, tb, dB);
   std::vector<PV> simplex;
   const int g = gjk(A, B, ta, tb, simplex, st);
+  if (st) st->flops = g_flops;
   if (g != COL_HIT) return g;
   V ca, cb;
   const int e = epa(simplex, A, B, &ca, &cb, st);
+  if (st) st->flops = g_flops;
   if (e != COL_HIT) return e;
   if (translate) {
     ca = add(ca, off);
     cb = add(cb, off);
   }
+  if (st) st->flops = g_flops;
   cp_a[0] = ca.x;
   cp_a[1] = ca.y;
   cp_a[2] = ca.z;

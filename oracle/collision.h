@@ -15,6 +15,7 @@ struct Stats {
   int tris = 0;       // triangles ever created
   int edges = 0;      // largest candidate edge list
   int heap = 0;       // largest heap
+  long long flops = 0;  // FP64 operations of the restated algorithm (add, sub, mul, div, sqrt = 1)
 };
 
 // Outcome codes.  1: in collision (cp_a, cp_b written); 0: no collision;

@@ -963,8 +963,8 @@ int oracle_dynamics(const gpb_model* m, int64_t inst, const double* q, const dou
 // for n pairs of cuboids: pose = (qx, qy, qz, qw, tx, ty, tz), dims = (w, d, h).
 // translate = 0 runs gjk / epa on the shapes where they are (the reference's
 // gjk / epa unit tests).  result[i] = orc_col outcome code; cp_a / cp_b are
-// written for hits; stats (6 ints per pair: GJK iterations, EPA expansions,
-// vertices, triangles, edges, heap size) may be NULL.
+// written for hits; stats (7 ints per pair: GJK iterations, EPA expansions,
+// vertices, triangles, edges, heap size, FP64 operations) may be NULL.
 int oracle_collide_cuboids(int64_t n, const double* pose_a, const double* dims_a, const double* pose_b,
                            const double* dims_b, int translate, int32_t* result, double* cp_a, double* cp_b,
                            int32_t* stats) {
@@ -977,8 +977,8 @@ int oracle_collide_cuboids(int64_t n, const double* pose_a, const double* dims_a
     result[i] = orc_col::collide(ra, pose_a + 7 * i + 4, dims_a + 3 * i, rb, pose_b + 7 * i + 4, dims_b + 3 * i,
                                  translate != 0, cp_a + 3 * i, cp_b + 3 * i, &st);
     if (stats) {
-      const int32_t v[6] = {st.gjk_iters, st.epa_iters, st.verts, st.tris, st.edges, st.heap};
-      for (int e = 0; e < 6; ++e) stats[6 * i + e] = v[e];
+      const int32_t v[7] = {st.gjk_iters, st.epa_iters, st.verts, st.tris, st.edges, st.heap, (int32_t)st.flops};
+      for (int e = 0; e < 7; ++e) stats[7 * i + e] = v[e];
     }
   }
   return 0;

@@ -11,7 +11,8 @@ distributions of its randomised collision tests.
   gjk_no_penetration, gjk_small_separation (gjk.rs:201-343) and
   epa_face_face_shallow_penetration (epa.rs:365-435), drawn from a seeded numpy
   generator instead of rand::rng().
-* ``pusher`` / ``gripper``: build_pusher / build_gripper (src/helpers.rs:559-666).
+* ``pusher`` / ``gripper`` / ``box_stack``: the builders of gpb.builders
+  (build_pusher / build_gripper, src/helpers.rs:559-666).
 """
 
 from __future__ import annotations
@@ -20,8 +21,6 @@ import math
 
 import numpy as np
 
-from gpb import (WORLD_FRAME, Cuboid, FloatingJoint, HalfSpace, MechanismState, PrismaticJoint,
-                 RevoluteJoint, RigidBody, SpatialInertia, Transform3D)
 from tests.golden.kats import quat_axis_angle, quat_euler
 
 PI = math.pi
@@ -139,91 +138,11 @@ def deep_pairs(rng, n):
 
 
 # ---------------------------------------------------------------------------
-# mechanisms with cuboid colliders
+# mechanisms with cuboid colliders: the package's builders (src/helpers.rs)
 
-def cuboid_body(frame, m, w, d, h, collider=True):
-    """RigidBody::new_cuboid (src/rigid_body.rs:160-173) + add_cuboid_collider."""
-    mom = np.diag([m * (d * d + h * h) / 12.0, m * (w * w + h * h) / 12.0, m * (w * w + d * d) / 12.0])
-    b = RigidBody(SpatialInertia(frame, mom, np.zeros(3), float(m)))
-    if collider:
-        b.add_cuboid_collider(Cuboid.new_at_center(w, d, h))
-    return b
-
-
-def _cube_with_contacts(state: MechanismState, frame: str, l: float):
-    """add_cube_contacts (src/helpers.rs:388-421)."""
-    from gpb import ContactPoint
-    h = l / 2.0
-    for c in [(h, h, -h), (h, -h, -h), (-h, h, -h), (-h, -h, -h),
-              (h, h, h), (h, -h, h), (-h, h, h), (-h, -h, h)]:
-        state.add_contact_point(ContactPoint(frame, c))
-
-
-def _cube_body(frame, m, l):
-    """RigidBody::new_cube (src/rigid_body.rs:147-158) + cube collider."""
-    mom = m * l * l / 6.0
-    b = RigidBody(SpatialInertia(frame, np.diag([mom] * 3), np.zeros(3), float(m)))
-    b.add_cuboid_collider(Cuboid.new_cube_at_center(l))
-    return b
-
-
-def pusher(ground=True):
-    """build_pusher (src/helpers.rs:559-607): revolute base, prismatic pusher
-    (cuboid collider), free cube (cuboid collider, 8 corner contacts)."""
-    wb, hb = 0.5, 0.5
-    base = cuboid_body("base", 1.0, wb, 0.5, hb, collider=False)
-    wp, dp, hp = 0.2, 0.2, 1.75
-    push = cuboid_body("pusher", 1.0, wp, dp, hp)
-    lc = 0.5
-    c = _cube_body("cube", 0.1, lc)
-    joints = [RevoluteJoint(Transform3D.move_xyz("base", WORLD_FRAME, 0.0, 0.0, 2.0), (0, 0, 1)),
-              PrismaticJoint(Transform3D.move_xyz("pusher", "base", wb / 2 + wp / 2, 0.0, -hb / 2 - hp / 2),
-                             (1, 0, 0)),
-              FloatingJoint(Transform3D.move_xyz("cube", WORLD_FRAME, wb + wp + 0.5, 0.0, lc / 2))]
-    s = MechanismState(joints, [base, push, c])
-    _cube_with_contacts(s, "cube", lc)
-    if ground:
-        s.add_halfspace(HalfSpace.new((0, 0, 1), 0.0))
-    return s
-
-
-def gripper(ground=True):
-    """build_gripper (src/helpers.rs:609-666): prismatic lift, two prismatic
-    jaws (cuboid colliders), free cube (cuboid collider, 8 corner contacts)."""
-    wl, dl, hl = 0.2, 0.2, 1.0
-    lift = cuboid_body("lift", 1.0, wl, dl, hl, collider=False)
-    wg, dg, hg = 0.1, 0.4, 0.4
-    left = cuboid_body("gripper_left", 0.5, wg, dg, hg)
-    right = cuboid_body("gripper_right", 0.5, wg, dg, hg)
-    lc = 0.5
-    c = _cube_body("cube", 0.1, lc)
-    joints = [PrismaticJoint(Transform3D.move_xyz("lift", WORLD_FRAME, 0.0, 0.0, 2.0), (0, 0, -1)),
-              PrismaticJoint(Transform3D.move_xyz("gripper_left", "lift", -wl / 2 - wg / 2 - 0.3, 0.0,
-                                                  -hl / 2 - hg / 2), (-1, 0, 0)),
-              PrismaticJoint(Transform3D.move_xyz("gripper_right", "lift", wl / 2 + wg / 2 + 0.3, 0.0,
-                                                  -hl / 2 - hg / 2), (1, 0, 0)),
-              FloatingJoint(Transform3D.move_xyz("cube", WORLD_FRAME, 0.0, 0.0, lc / 2))]
-    s = MechanismState(joints, [lift, left, right, c])
-    _cube_with_contacts(s, "cube", lc)
-    if ground:
-        s.add_halfspace(HalfSpace.new((0, 0, 1), 0.0))
-    return s
-
-
-def box_stack(n_boxes=3, ground=True):
-    """Free cuboids (each a FloatingJoint to the world, each with a collider and
-    its 8 corners as contact points) — every pair is tested."""
-    joints, bodies = [], []
-    for k in range(n_boxes):
-        f = f"box{k}"
-        joints.append(FloatingJoint(Transform3D(f, WORLD_FRAME)))
-        bodies.append(_cube_body(f, 1.0, 0.5))
-    s = MechanismState(joints, bodies)
-    for k in range(n_boxes):
-        _cube_with_contacts(s, f"box{k}", 0.5)
-    if ground:
-        s.add_halfspace(HalfSpace.new((0, 0, 1), 0.0))
-    return s
+from gpb.builders import build_box_stack as box_stack  # noqa: E402
+from gpb.builders import build_gripper as gripper  # noqa: E402
+from gpb.builders import build_pusher as pusher  # noqa: E402
 
 
 def unit_quats(rng, n, scale):

@@ -123,13 +123,13 @@ def test_oracle_storage_high_water_marks(built):
     """The kernel's fixed storage (48 vertices, 160 faces, 32 edges, 64 GJK
     iterations) is far above what these distributions reach."""
     rng = np.random.default_rng(3)
-    worst = np.zeros(6, int)
+    worst = np.zeros(7, int)
     for gen in (cb.shallow_face_pairs, cb.epa_face_pairs, cb.deep_pairs):
         pa, da, pb, db = gen(rng, 20000)
         r, _, _, st = oracle.collide_cuboids(pa, da, pb, db, stats=True)
         assert np.all(r >= 0)
         worst = np.maximum(worst, st.max(0))
-    gjk, _, verts, tris, edges, _ = worst
+    gjk, _, verts, tris, edges, _, _ = worst
     assert gjk < 64 and verts < 48 and tris < 160 and edges < 32, worst
 
 

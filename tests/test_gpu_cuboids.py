@@ -17,57 +17,14 @@ import pytest
 
 import gpb
 import oracle
-from gpb import Batch, Model
+from gpb import Batch, Model, builders
 from tests.golden import cuboids as cb
-
-
-def gripper_states(rng, n, closed=True):
-    """q = (lift, left jaw, right jaw, cube pose): jaws 0.02-0.07 into the cube
-    (or 0.1 apart when not `closed`), the cube resting near the ground with a
-    small random rotation; random velocities."""
-    q = np.zeros((n, 10))
-    q[:, 0] = rng.uniform(0.95, 1.05, n)
-    lo, hi = (-0.22, -0.17) if closed else (0.05, 0.1)
-    q[:, 1] = rng.uniform(lo, hi, n)
-    q[:, 2] = rng.uniform(lo, hi, n)
-    q[:, 3:7] = cb.unit_quats(rng, n, 0.05)
-    q[:, 7:9] = rng.uniform(-0.01, 0.01, (n, 2))
-    q[:, 9] = rng.uniform(-0.01, 0.01, n)
-    v = rng.normal(0, 0.1, (n, 9))
-    return q, v
-
-
-def pusher_states(rng, n):
-    """q = (base angle, pusher slide, cube pose): the pusher's lower end pressed
-    0.01-0.05 into the cube's face."""
-    q = np.zeros((n, 9))
-    q[:, 0] = rng.uniform(-0.05, 0.05, n)
-    # pusher x (at slide s): 0.35 + s; its face at 0.45 + s; the cube's face at 0.95
-    q[:, 1] = rng.uniform(0.51, 0.55, n)
-    q[:, 2:6] = cb.unit_quats(rng, n, 0.05)
-    q[:, 6:8] = rng.uniform(-0.01, 0.01, (n, 2))
-    q[:, 8] = rng.uniform(-0.01, 0.01, n)
-    v = rng.normal(0, 0.1, (n, 8))
-    return q, v
-
-
-def stack_states(rng, n, k=3):
-    """k free unit-mass cubes (0.5 m) stacked along z with 0.005-0.03 overlaps,
-    jittered in x, y and rotation."""
-    q = np.zeros((n, 7 * k))
-    z = np.full(n, 0.25 - 0.002)
-    for b in range(k):
-        q[:, 7 * b:7 * b + 4] = cb.unit_quats(rng, n, 0.1)
-        q[:, 7 * b + 4:7 * b + 6] = rng.uniform(-0.1, 0.1, (n, 2))
-        q[:, 7 * b + 6] = z
-        z = z + 0.5 - rng.uniform(0.005, 0.03, n)
-    v = rng.normal(0, 0.2, (n, 6 * k))
-    return q, v
 
 
 def build(kind, n, rng, **kw):
     mech = {"gripper": cb.gripper, "pusher": cb.pusher, "stack": cb.box_stack}[kind]()
-    states = {"gripper": gripper_states, "pusher": pusher_states, "stack": stack_states}[kind]
+    states = {"gripper": builders.gripper_states, "pusher": builders.pusher_states,
+              "stack": builders.box_stack_states}[kind]
     M = Model.from_mechanisms([mech] * n)
     q, v = states(rng, n, **kw)
     return M, q, v

@@ -175,3 +175,49 @@ def test_request_fitting_no_class_is_rejected(ctx):
     with pytest.raises(gpb.GpbError, match="fits no slot class"):
         S.submit(M, 0, 1, q0, v0, dt=1e-3, steps=10)
     S.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algorithm", [gpb.ALGO_CRBA, gpb.ALGO_ABA])
+def test_cuboid_requests_alone_mix_and_batch(ctx, algorithm):
+    """build_gripper requests (3 GJK/EPA pair queries per evaluation) in a class
+    with max_cuboids = 3, mixed with chains: alone == mix, bit for bit, and both
+    equal the batch API."""
+    from gpb import builders
+
+    n = 12
+    Mg = Model.from_mechanisms([builders.build_gripper()] * n)
+    qg, vg = builders.gripper_states(np.random.default_rng(8), n)
+    Mc, qc, vc, _ = Model.from_config(1, 10, seed=4)
+    M = Model.concat([Mg, Mc])
+    q0 = np.concatenate([qg.ravel(), qc])
+    v0 = np.concatenate([vg.ravel(), vc])
+    qo, vo, _ = M.offsets()
+    classes = [SlotClass(4, 10, 9, 8, 1, packs=1, max_cuboids=3), SlotClass(48, 48, 48, packs=1)]
+
+    def run(idx, chunk):
+        S = Server(ctx, classes, precision=gpb.FP64, chunk_steps=chunk, algorithm=algorithm)
+        ids = {}
+        for i in idx:
+            grip = i < n
+            rid = S.submit(M, int(i), 1, q0, v0, dt=1e-5 if grip else 5e-4, steps=60 + 7 * (i % 5),
+                           control="host" if grip else "open_loop", seed=3 + i, keys=0)
+            ids[i] = int(rid[0])
+        S.drain(100000)
+        out = {i: S.result(r) for i, r in ids.items()}
+        S.close()
+        return out
+
+    mix = run(list(range(M.n)), 23)
+    for i in (0, 5, 11, 13):
+        alone = run([i], 41)[i]
+        assert alone[2] == mix[i][2] == 0
+        assert np.array_equal(alone[0], mix[i][0]) and np.array_equal(alone[1], mix[i][1]), i
+    for i in (2, 9):
+        B = Batch(M.subset([i]), ctx)
+        B.set_algorithm(algorithm)
+        B.update(q0[qo[i]:qo[i + 1]], v0[vo[i]:vo[i + 1]])
+        B.simulate_steps(60 + 7 * (i % 5), 1e-5, 0, gpb.FP64)
+        qb, vb = B.state()
+        B.close()
+        assert np.array_equal(qb, mix[i][0]) and np.array_equal(vb, mix[i][1]), i
