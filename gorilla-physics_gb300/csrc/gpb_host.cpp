@@ -139,6 +139,7 @@ int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
       return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": more than " +
                                    std::to_string(GPB_MAX_CUBOIDS) + " cuboid colliders");
   }
+  I.mvs = I.nc * I.nh + I.nu * (I.nu - 1) / 2;
   sig = (sig ^ (uint64_t)(I.nc * 7 + I.nh + 1000 * I.nu)) * 1099511628211ull;
   I.sig = sig;
   return GPB_OK;
@@ -183,7 +184,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
   const int64_t npacks = (n + LANES - 1) / LANES;
   B->npacks = (int32_t)npacks;
   B->packs_h.resize(npacks);
-  int64_t rt = 0, rc = 0, rh = 0, rq = 0, rv = 0, rl = 0, rs = 0;
+  int64_t rt = 0, rc = 0, rh = 0, rq = 0, rv = 0, rl = 0, rs = 0, rvs = 0;
   for (int64_t p = 0; p < npacks; ++p) {
     PackDesc& P = B->packs_h[p];
     std::memset(&P, 0, sizeof(P));
@@ -198,6 +199,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
       P.nc = std::max(P.nc, I.nc);
       P.nh = std::max(P.nh, I.nh);
       P.nu = std::max(P.nu, I.nu);
+      P.mvs = std::max(P.mvs, I.mvs);
       P.minnv = std::min(P.minnv, I.nv);
       if (!I.chain) P.chain = 0;
     }
@@ -208,6 +210,8 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
     P.v = rv;
     P.lane = rl;
     P.scr = rs;
+    P.vs = rvs;
+    if (P.mvs <= GPB_MAX_VS_CONTACTS) rvs += vs_layout(P.nv, P.mvs).total;
     rt += P.nb;
     rc += P.nc;
     rh += P.nh;
@@ -261,6 +265,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
     if (x != cudaSuccess && e == cudaSuccess) e = x;
   };
   B->scratch_words = rs * L;
+  B->vs_rows = rvs;
   B->q_slots = rq * L;
   B->v_slots = rv * L;
   B->c_slots = rc * 3 * L;
@@ -435,7 +440,7 @@ extern "C" int gpb_get_state(gpb_batch* b, double* q, double* v) {
 }
 
 static int check_enums(int integrator, int precision) {
-  if (integrator < 0 || integrator > 2) return fail(GPB_E_INVAL, "unknown integrator");
+  if (integrator < 0 || integrator > 3) return fail(GPB_E_INVAL, "unknown integrator");
   if (precision != GPB_FP64 && precision != GPB_MIXED && precision != GPB_MIXED_REFINED)
     return fail(GPB_E_INVAL, "unknown precision");
   return GPB_OK;
@@ -500,6 +505,19 @@ static int run_simulate(gpb_batch* b, double dt, int64_t K, int64_t step0, int i
                         double* history) {
   if (int r = check_enums(integrator, precision)) return r;
   if (K < 0) return fail(GPB_E_INVAL, "negative step count");
+  if (integrator == GPB_VELOCITY_STEPPING) {  // FP64 only; its scratch on first use
+    if (precision != GPB_FP64) return fail(GPB_E_INVAL, "velocity stepping runs in GPB_FP64 only");
+    for (const PackDesc& P : b->packs_h)
+      if (P.mvs > GPB_MAX_VS_CONTACTS)
+        return fail(GPB_E_RANGE, "velocity stepping: an instance has more than " +
+                                     std::to_string(GPB_MAX_VS_CONTACTS) +
+                                     " potential contacts (contact points x half-spaces + cuboid pairs)");
+    if (b->vs_rows > 0 && !b->vscratch.p) {
+      CUDA_TRY(cudaSetDevice(b->ctx->device));
+      if (b->vscratch.alloc((size_t)b->vs_rows * LANES) != cudaSuccess)
+        return fail(GPB_E_NOMEM, "velocity stepping: scratch allocation failed");
+    }
+  }
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(GPB_E_INVAL, "dt must be positive and finite");
   CUDA_TRY(cudaSetDevice(b->ctx->device));
   cudaStream_t s = b->ctx->stream;

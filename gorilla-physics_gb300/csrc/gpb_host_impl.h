@@ -55,6 +55,7 @@ struct DBuf {
 // Validated shape of one instance of a gpb_model.
 struct InstInfo {
   int32_t j0, nb, nq, nv, c0, nc, h0, nh, model, nu;
+  int32_t mvs;  // velocity stepping: potential contacts (points × half-spaces + cuboid pairs)
   bool chain;
   uint64_t sig;  // topology class
 };
@@ -214,10 +215,11 @@ struct gpb_batch {
   std::vector<gpb::PackDesc> packs_h;
   int64_t q_slots = 0, v_slots = 0, c_slots = 0;
   int64_t scratch_words = 0;  // 8-byte words of per-instance scratch, all packs
+  int64_t vs_rows = 0;        // rows of velocity-stepping scratch, all packs (allocated on first use)
   std::vector<int32_t> status_slot;  // user instance -> status slot (pack*32+lane)
   gpb::DBuf<gpb::PackDesc> packs;
   gpb::DBuf<uint32_t> topoW;
-  gpb::DBuf<double> topoD, ctcD, hsD, q, v, tau_in, scratch, stage_q, stage_v, stage_c, hist;
+  gpb::DBuf<double> topoD, ctcD, hsD, q, v, tau_in, scratch, stage_q, stage_v, stage_c, hist, vscratch;
   gpb::DBuf<float> topoF, ctcF, hsF;
   gpb::DBuf<int32_t> ctcI, laneI, status, queue;
   gpb::DBuf<int64_t> qmap, vmap, cmap, done;
@@ -250,6 +252,7 @@ struct gpb_batch {
     b.queue = queue.p;
     b.algorithm = algorithm;
     b.gravity = gravity;
+    b.vscratch = vscratch.p;
     return b;
   }
   void release() {
@@ -262,6 +265,7 @@ struct gpb_batch {
     v.free();
     tau_in.free();
     scratch.free();
+    vscratch.free();
     stage_q.free();
     stage_v.free();
     stage_c.free();

@@ -46,7 +46,9 @@ constexpr int LANE_I = 8;   // per-lane ints: instance, nb, nq, nv, nc, nh, cont
 
 struct PackDesc {
   int32_t count, nb, nq, nv, nc, nh, chain, minnv;  // minnv: smallest DOF count of its lanes
-  int32_t nu, pad_;  // nu: largest cuboid-collider count of its lanes
+  int32_t nu;   // largest cuboid-collider count of its lanes
+  int32_t mvs;  // velocity stepping: largest potential contact count of its lanes
+                // (points × half-spaces + cuboid pairs), 0 = none
   // bases in rows (one row = LANES elements)
   int64_t topo;   // topology bodies (2 int words / TOPO_D reals per body)
   int64_t ctc;    // contacts
@@ -54,6 +56,7 @@ struct PackDesc {
   int64_t q, v;   // state (doubles)
   int64_t lane;   // per-lane ints
   int64_t scr;    // scratch, in rows of 8-byte words
+  int64_t vs;     // velocity-stepping scratch, in rows of 8-byte words
 };
 
 // Scratch sub-array offsets (rows of 8-byte words; R-typed arrays use the same
@@ -86,6 +89,50 @@ __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, 
   s.tau = o; o += nv;
   s.cf = o; o += 3 * nc;
   s.U = o; o += nu > 1 ? UREC_D * nu : 0;  // cuboid records (pairs need two)
+  s.total = o;
+  return s;
+}
+
+// Velocity-stepping scratch of one pack (rows of 8-byte words, lane-interleaved),
+// for up to mc contacts (m = 3 mc rows of the contact Jacobian) and nv DOF.
+struct VSLayout {
+  int32_t mc, m;
+  int32_t ct;              // contacts: normal (3), point (3), body a, body b
+  int32_t J, Y;            // J (m × nv, row-major) and Y = (M⁻¹ Jᵀ)ᵀ (m × nv)
+  int32_t P, H;            // the scaled program's P and the Newton matrix (m × m)
+  int32_t W, Wi, eta;      // per cone: NT scaling W, W⁻¹ (9 each), η
+  int32_t qv, y, z, r, lam, dya, dza, dy, dz, rs, rhs, ds;  // m each
+  int32_t vf, qdd;         // nv each: free velocity, its acceleration
+  int32_t total;
+};
+__host__ __device__ inline VSLayout vs_layout(int nv, int mc) {
+  VSLayout s;
+  const int m = 3 * mc;
+  int o = 0;
+  s.mc = mc;
+  s.m = m;
+  s.ct = o; o += 8 * mc;
+  s.J = o; o += m * nv;
+  s.Y = o; o += m * nv;
+  s.P = o; o += m * m;
+  s.H = o; o += m * m;
+  s.W = o; o += 9 * mc;
+  s.Wi = o; o += 9 * mc;
+  s.eta = o; o += mc;
+  s.qv = o; o += m;
+  s.y = o; o += m;
+  s.z = o; o += m;
+  s.r = o; o += m;
+  s.lam = o; o += m;
+  s.dya = o; o += m;
+  s.dza = o; o += m;
+  s.dy = o; o += m;
+  s.dz = o; o += m;
+  s.rs = o; o += m;
+  s.rhs = o; o += m;
+  s.ds = o; o += m;
+  s.vf = o; o += nv;
+  s.qdd = o; o += nv;
   s.total = o;
   return s;
 }
@@ -136,6 +183,7 @@ struct DeviceBatch {
   int32_t algorithm;       // GPB_ALGO_CRBA or GPB_ALGO_ABA
   double gravity;          // m/s² along −z (9.81 unless set)
   int32_t plain;           // 1: no contact points, no prismatic springs (free_velocity)
+  double* vscratch;        // velocity-stepping scratch (PackDesc::vs), null until first used
   // serving pool only (all null for a batch)
   LaneJob* jobs;           // per-slot jobs
   const int32_t* active;   // packs to run in this launch (nactive of them)

@@ -69,6 +69,7 @@ struct LaneCtx {
   int lane, nb, nq, nv, nc, nh, model, chain;
   int nu;       // cuboid colliders (slots 1..nu in body order)
   int springs;  // prismatic springs act (off for Articulated::free_velocity)
+  int allx;     // keep every body's world pose in X (velocity stepping)
   double grav;  // gravitational acceleration along −z
   const uint32_t* W;  // topology words (row base applied, lane applied)
   const R* T;         // topology reals
@@ -726,7 +727,7 @@ __device__ __noinline__ int lane_sweeps(const LaneCtx<R>& cin, Col<double> q, Co
                    V3<double>{double(Vb.w.x), double(Vb.w.y), double(Vb.w.z)},
                    V3<double>{double(Vb.v.x), double(Vb.v.y), double(Vb.v.z)});
     }
-    if (fl & BF_BRANCH) {
+    if (fl & BF_BRANCH || c.allx) {
 #pragma unroll
       for (int k = 0; k < 9; ++k) c.r(c.L.X + 12 * b + k) = Rb.a[k];
       c.r(c.L.X + 12 * b + 9) = pb.x;
@@ -949,6 +950,8 @@ __device__ __forceinline__ void advance_q(const LaneCtx<R>& c, Col<double> q, Co
   }
 }
 
+#include "gpb_vstep.cuh"
+
 // Dynamics evaluators of the three precision modes (q, v, τ → q̈).
 struct EvalFP64 {
   LaneCtx<double> c;
@@ -1047,11 +1050,12 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   c.nq = li[2 * LANES];
   c.nv = li[3 * LANES];
   c.nc = b.plain ? 0 : li[4 * LANES];  // free_velocity: no contact points
-  c.nh = li[5 * LANES];
+  c.nh = b.plain ? 0 : li[5 * LANES];
   c.model = li[6 * LANES];
   c.nu = b.plain ? 0 : li[7 * LANES];  // free_velocity: no colliders
   c.chain = pd.chain;
   c.springs = b.plain ? 0 : 1;
+  c.allx = 0;
   c.grav = b.gravity;
   c.W = b.topoW + pd.topo * 2 * LANES + lane;
   c.T = RealTopo<R>::topo(b) + pd.topo * TOPO_D * LANES + lane;
@@ -1179,7 +1183,14 @@ __global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams
       const int64_t sidx = lp.step0 + s;
       bool ht = control(c, b, lp, inst, sidx, s == 0, q, v, tin, tau);
       Col<double> tsrc = lp.control == 0 ? tin : tau;
-      const int st = lane_step(ev, q, v, tsrc, ht, lp.dt, lp.integrator);
+      int st;
+      if constexpr (PREC == 0) {  // velocity stepping runs in FP64 only (checked on the host)
+        st = lp.integrator == 3 ? vstep::lane_velocity_step(c, vstep::View{b.vscratch + pd.vs * LANES + lane},
+                                                             vs_layout(pd.nv, pd.mvs), q, v, tsrc, ht, lp.dt)
+                                : lane_step(ev, q, v, tsrc, ht, lp.dt, lp.integrator);
+      } else {
+        st = lane_step(ev, q, v, tsrc, ht, lp.dt, lp.integrator);
+      }
       if (st) {
         *status = st;
         break;

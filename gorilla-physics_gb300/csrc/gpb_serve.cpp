@@ -385,7 +385,8 @@ extern "C" int gpb_server_submit(gpb_server* S, const gpb_model* m, int64_t firs
     if (!(rq.dt > 0.0) || !std::isfinite(rq.dt) || rq.steps < 1 || rq.integrator < 0 || rq.integrator > 2 ||
         rq.control < 0 || rq.control > 2)
       return fail(GPB_E_INVAL, "gpb_server_submit: request " + std::to_string(k) +
-                                   ": dt > 0, steps >= 1 and a known integrator / control are required");
+                                   ": dt > 0, steps >= 1 and a known integrator / control are required "
+                                   "(velocity stepping is not served)");
     // smallest class that fits
     int best = -1;
     for (int c = 0; c < (int)S->classes.size(); ++c) {

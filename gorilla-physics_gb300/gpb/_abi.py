@@ -14,9 +14,9 @@ LIB_PATH = Path(__file__).resolve().parent / "libgpb.so"
 # return codes / status bits / enums (include/gpb.h)
 GPB_OK = 0
 GPB_E_INVAL, GPB_E_NOMEM, GPB_E_CUDA, GPB_E_TIMEOUT, GPB_E_RANGE, GPB_E_STATE = -1, -2, -3, -4, -5, -6
-GPB_ST_NONFINITE, GPB_ST_CHOL_FAIL, GPB_ST_COLLISION = 1, 2, 4
+GPB_ST_NONFINITE, GPB_ST_CHOL_FAIL, GPB_ST_COLLISION, GPB_ST_SOLVER = 1, 2, 4, 8
 FIXED, REVOLUTE, PRISMATIC, FLOATING = 0, 1, 2, 3
-SEMI_IMPLICIT_EULER, RUNGE_KUTTA_2, RUNGE_KUTTA_4 = 0, 1, 2
+SEMI_IMPLICIT_EULER, RUNGE_KUTTA_2, RUNGE_KUTTA_4, VELOCITY_STEPPING = 0, 1, 2, 3
 FP64, MIXED, MIXED_REFINED = 0, 1, 2
 ALGO_CRBA, ALGO_ABA = 0, 1
 HUNT_CROSSLEY, LINEAR_SPRING_DAMPER = 0, 1

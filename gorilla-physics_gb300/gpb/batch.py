@@ -21,6 +21,7 @@ Integrator = type("Integrator", (), {
     "SemiImplicitEuler": _abi.SEMI_IMPLICIT_EULER,
     "RungeKutta2": _abi.RUNGE_KUTTA_2,
     "RungeKutta4": _abi.RUNGE_KUTTA_4,
+    "VelocityStepping": _abi.VELOCITY_STEPPING,
 })
 Precision = type("Precision", (), {"FP64": _abi.FP64, "MIXED": _abi.MIXED})
 

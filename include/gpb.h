@@ -58,6 +58,9 @@ extern "C" {
 #define GPB_ST_CHOL_FAIL 2 /* mass matrix not positive definite            */
 #define GPB_ST_COLLISION 4 /* cuboid GJK/EPA met a case the reference panics
                               on, or ran past its loop / storage bounds   */
+#define GPB_ST_SOLVER 8    /* velocity stepping: the friction-cone program
+                              did not converge (the reference panics on a
+                              NaN impulse)                                */
 
 /* ---- enums ------------------------------------------------------------ */
 /* Joint kinds of src/joint/mod.rs:21-27. */
@@ -68,12 +71,21 @@ enum gpb_joint_type {
   GPB_JOINT_FLOATING = 3
 };
 
-/* Continuous integrators of src/integrators.rs:17-23 (the velocity-stepping
- * variants solve a conic program and are not part of this library). */
+/* Integrators of src/integrators.rs:17-23.  GPB_VELOCITY_STEPPING is
+ * velocity_stepping (src/integrators.rs:42-51, dynamics_discrete
+ * src/dynamics.rs:367-430): v_free = v + dt M⁻¹(τ − c) without contact
+ * wrenches, every contact (points and spheres against half-spaces, cuboid
+ * pairs) a friction cone (μ = 0.95) of the impulse program
+ * min ½λᵀ(J M⁻¹ Jᵀ)λ + (J v_free)ᵀλ (src/dynamics.rs:652-742, solved on the
+ * device by a primal-dual interior-point method), v' = v_free + M⁻¹Jᵀλ,
+ * q' = q + dt v' (compute_new_q).  FP64 only; at most GPB_MAX_VS_CONTACTS
+ * potential contacts per instance (points × half-spaces + cuboid pairs).
+ * The CCD variant is not provided. */
 enum gpb_integrator {
   GPB_SEMI_IMPLICIT_EULER = 0,
   GPB_RUNGE_KUTTA_2 = 1,
-  GPB_RUNGE_KUTTA_4 = 2
+  GPB_RUNGE_KUTTA_4 = 2,
+  GPB_VELOCITY_STEPPING = 3
 };
 
 /* GPB_FP64: every quantity in FP64 (the drop-in).  GPB_MIXED: sweeps, contact
@@ -173,6 +185,7 @@ typedef struct gpb_model {
 #define GPB_MAX_CONTACTS 64
 #define GPB_MAX_HALFSPACES 4
 #define GPB_MAX_CUBOIDS 8
+#define GPB_MAX_VS_CONTACTS 16
 
 /* ---- library / context ------------------------------------------------ */
 typedef struct gpb_ctx gpb_ctx;

@@ -19,7 +19,7 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 LIB = HERE / "liboracle.so"
 SRC = HERE / "gpb_oracle.cpp"
-SOURCES = (SRC, HERE / "collision.cpp")
+SOURCES = (SRC, HERE / "collision.cpp", HERE / "socp.cpp")
 
 P_f64 = C.POINTER(C.c_double)
 P_i64 = C.POINTER(C.c_int64)
@@ -30,7 +30,7 @@ LU, CHOLESKY = 0, 1
 
 def build(force: bool = False) -> Path:
     """g++ -O2 -ffp-contract=off (x86 and Arm agree bit for bit)."""
-    deps = [*SOURCES, HERE / "collision.h", REPO / "include/gpb.h"]
+    deps = [*SOURCES, HERE / "collision.h", HERE / "socp.h", REPO / "include/gpb.h"]
     if force or not LIB.exists() or LIB.stat().st_mtime < max(p.stat().st_mtime for p in deps):
         tmp = LIB.with_suffix(".so.tmp")
         subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
@@ -55,6 +55,9 @@ def lib():
         L.oracle_free_velocity.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_double, C.c_int, P_f64]
         L.oracle_collide_cuboids.argtypes = [C.c_int64, P_f64, P_f64, P_f64, P_f64, C.c_int, P_i32,
                                              P_f64, P_f64, P_i32]
+        L.oracle_vs_step.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_double, C.c_int, P_i32,
+                                     P_f64, P_f64, P_f64, P_f64, P_f64]
+        L.oracle_socp_solve.argtypes = [C.c_int, P_f64, P_f64, C.c_double, P_f64, P_f64]
         L.oracle_energy.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, P_f64]
         L.oracle_step.argtypes = [vp, C.c_int64, P_f64, P_f64, P_f64, C.c_double, C.c_int, C.c_int]
         L.oracle_open_loop_tau.argtypes = [C.c_uint32, C.c_int64, C.c_int64, C.c_int32, C.c_double]
@@ -133,6 +136,40 @@ def collide_cuboids(pose_a, dims_a, pose_b, dims_b, translate=True, stats=False)
     lib().oracle_collide_cuboids(n, _p(pa), _p(da), _p(pb), _p(db), int(bool(translate)),
                                  res.ctypes.data_as(P_i32), _p(ca), _p(cb), stt.ctypes.data_as(P_i32))
     return (res, ca, cb, stt) if stats else (res, ca, cb)
+
+
+VELOCITY_STEPPING = 3
+
+
+def vs_step(model, i, q, v, dt, tau=None, max_contacts=64):
+    """One velocity-stepping step of instance i with its program (src/dynamics.rs:367-430,
+    652-742).  Returns dict(q, v, status, nc, J, M, vfree, lam, vnext)."""
+    _, nv, _, q, v, t = _checked(model, i, q, v, tau)
+    q, v = q.copy(), v.copy()
+    nc = C.c_int32()
+    m = 3 * max_contacts
+    J = np.zeros(max(m * nv, 1))
+    Mm = np.zeros(max(nv * nv, 1))
+    vf, vn = np.zeros(max(nv, 1)), np.zeros(max(nv, 1))
+    lam = np.zeros(max(m, 1))
+    st = lib().oracle_vs_step(_m(model), i, _p(q), _p(v), _p(t), dt, max_contacts, C.byref(nc), _p(J),
+                              _p(Mm), _p(vf), _p(lam), _p(vn))
+    k = nc.value
+    return dict(q=q, v=v, status=st, nc=k, J=J[:3 * k * nv].reshape(3 * k, nv), M=Mm[:nv * nv].reshape(nv, nv),
+                vfree=vf[:nv], lam=lam[:3 * k], vnext=vn[:nv])
+
+
+def socp_solve(G, g, mu=0.95):
+    """The velocity-stepping friction-cone program (src/dynamics.rs:652-742):
+    minimise ½λᵀGλ + gᵀλ with ‖(λ_t, λ_b)‖ ≤ μ λ_n per contact.  Returns
+    (λ, status, (iterations, residual, gap))."""
+    G = np.ascontiguousarray(G, float)
+    g = np.ascontiguousarray(g, float).ravel()
+    nc = g.size // 3
+    lam = np.zeros(max(g.size, 1))
+    info = np.zeros(3)
+    st = lib().oracle_socp_solve(nc, _p(G), _p(g), mu, _p(lam), _p(info))
+    return lam[:g.size], st, tuple(info)
 
 
 def mass_matrix(model, i, q):

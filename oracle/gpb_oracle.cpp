@@ -32,6 +32,7 @@
 
 #include "collision.h"
 #include "gpb.h"
+#include "socp.h"
 
 namespace orc {
 
@@ -802,10 +803,202 @@ static void sie_step(const Mechanism& M, const double* q, const double* v, const
   }
 }
 
+// ---------------------------------------------------------------------------
+// Velocity stepping (src/integrators.rs:42-51; dynamics_discrete,
+// src/dynamics.rs:367-430; collision_detection 520-650;
+// solve_constraint_and_contact 652-742; compose_contact_jacobian 744-820).
+
+struct VSContact {
+  V3 n, p;   // contact normal (towards body a), contact point (world)
+  int a, b;  // body numbers (1-based); b = 0: a static half-space
+};
+
+// collision_detection: points inside a half-space (margin 1e-8), spheres
+// within their radius (contact at the centre's projection, Sphere::contact_halfspace,
+// src/collision/sphere.rs:27-34), then cuboid pairs (normal cp_b − cp_a, point cp_a).
+static int vs_contacts(const Mechanism& M, const std::vector<Iso>& X, std::vector<VSContact>& out) {
+  const int n = (int)M.joints.size();
+  out.clear();
+  for (int pass = 0; pass < 2; ++pass)  // ContactPoints, then sphere colliders
+    for (int a = 0; a < n; ++a) {
+      const M3 R = to_rotation_matrix(X[a + 1].r);
+      for (const Contact& cp : M.contacts[a]) {
+        if ((cp.radius > 0.0) != (pass == 1)) continue;
+        const V3 loc = mul(R, cp.loc) + X[a + 1].t;
+        for (const HalfSpace& h : M.halfspaces) {
+          const double d = dot(loc - h.point, h.normal);
+          if (pass == 0) {
+            if (d <= 1e-8) out.push_back({h.normal, loc, a + 1, 0});
+          } else if (d <= cp.radius) {
+            out.push_back({h.normal, loc - h.normal * d, a + 1, 0});
+          }
+        }
+      }
+    }
+  for (int a = 0; a < n; ++a) {
+    if (!M.cuboid[a]) continue;
+    for (int b = a + 1; b < n; ++b) {
+      if (!M.cuboid[b]) continue;
+      const M3 Ra = to_rotation_matrix(X[a + 1].r), Rb = to_rotation_matrix(X[b + 1].r);
+      double ra[9], rb[9];
+      for (int e = 0; e < 9; ++e) {
+        ra[e] = Ra.m[e / 3][e % 3];
+        rb[e] = Rb.m[e / 3][e % 3];
+      }
+      const double ta[3] = {X[a + 1].t.x, X[a + 1].t.y, X[a + 1].t.z};
+      const double tb[3] = {X[b + 1].t.x, X[b + 1].t.y, X[b + 1].t.z};
+      double ca[3], cb[3];
+      const int r = orc_col::collide(ra, ta, &M.cuboid_dims[3 * (size_t)a], rb, tb, &M.cuboid_dims[3 * (size_t)b],
+                                     true, ca, cb, nullptr);
+      if (r < 0) return GPB_ST_COLLISION;
+      if (r != orc_col::COL_HIT) continue;
+      const V3 pa{ca[0], ca[1], ca[2]}, pb{cb[0], cb[1], cb[2]};
+      const V3 d = pb - pa;
+      const double nd = norm(d);
+      out.push_back({{d.x / nd, d.y / nd, d.z / nd}, pa, a + 1, b + 1});
+    }
+  }
+  return 0;
+}
+
+static V3 unit(V3 a) {
+  const double n = norm(a);
+  return {a.x / n, a.y / n, a.z / n};
+}
+
+// One velocity-stepping step in place.  Returns status bits; *ncontacts and
+// the program's iteration count go to info (may be NULL).
+struct VSDetails {  // the program of one step (for tests)
+  int nc = 0, iterations = 0;
+  std::vector<double> J, Mm, vfree, lambda, vnext;
+};
+
+static int velocity_step(const Mechanism& M, double* q, double* v, const double* tau, double dt, Work& w,
+                         int* info, VSDetails* det = nullptr) {
+  const int n = (int)M.joints.size(), nv = M.nv;
+  bodies_to_root(M, q, w.X);
+  w.jt.resize(n);
+  for (int a = 0; a < n; ++a) w.jt[a] = joint_twist(M.joints[a], v);
+  w.T.assign(n + 1, SV{{0, 0, 0}, {0, 0, 0}});
+  for (int a = 0; a < n; ++a) w.T[a + 1] = sv_add(w.T[M.joints[a].parent], twist_transform(w.jt[a], w.X[a + 1]));
+  mass_matrix(M, w.X, w.M);
+  w.Wc.assign(n + 1, SV{{0, 0, 0}, {0, 0, 0}});  // no explicit contact wrenches
+  dynamics_bias(M, w.X, w.jt, w.T, w.Wc, w.c);
+  std::vector<double> t(nv);
+  for (int i = 0; i < nv; ++i) t[i] = tau ? tau[i] : 0.0;
+  for (int a = 0; a < n; ++a) {  // add_prismatic_joint_spring_force
+    const Joint& J = M.joints[a];
+    if (J.type == GPB_JOINT_PRISMATIC && J.spring_k != 0.0) t[J.vo] = t[J.vo] + (-J.spring_k * (q[J.qo] - J.spring_l));
+  }
+  if (nv == 0) return 0;
+  // v_free = v + M⁻¹ (τ dt − c dt)   (dynamics_solve(M, c·dt, τ·dt))
+  std::vector<double> vf(nv);
+  for (int i = 0; i < nv; ++i) vf[i] = t[i] * dt - w.c[i] * dt;
+  if (!lu_solve(w.M, nv, vf)) return GPB_ST_CHOL_FAIL;
+  for (int i = 0; i < nv; ++i) vf[i] = v[i] + vf[i];
+  // contacts and their 3-row Jacobians C X H
+  std::vector<VSContact> cts;
+  if (int st = vs_contacts(M, w.X, cts)) return st;
+  const int nc = (int)cts.size(), m = 3 * nc;
+  if (info) info[0] = nc;
+  std::vector<double> vn(vf);
+  if (nc > 0) {
+    std::vector<std::vector<SV>> S(n, std::vector<SV>(6));
+    std::vector<int> dim(n);
+    for (int a = 0; a < n; ++a) {  // build_jacobian_blocks: world motion-subspace columns
+      dim[a] = motion_subspace(M.joints[a], S[a].data());
+      jacobian_transform(S[a].data(), dim[a], w.X[a + 1]);
+    }
+    std::vector<double> Jm((size_t)m * nv, 0.0);
+    for (int k = 0; k < nc; ++k) {
+      const VSContact& c = cts[k];
+      V3 cand = cross(c.n, V3{1, 0, 0});
+      const V3 tt = norm(cand) != 0.0 ? unit(cand) : unit(cross(c.n, V3{0, 1, 0}));
+      const V3 bb = unit(cross(c.n, tt));
+      std::vector<int> ca(n + 1, 0), cb(n + 1, 0);
+      for (int x = c.a; x != 0; x = M.joints[x - 1].parent) ca[x] = 1;
+      for (int x = c.b; x != 0; x = M.joints[x - 1].parent) cb[x] = 1;
+      for (int a = 0; a < n; ++a) {
+        const double sg = ca[a + 1] ? 1.0 : (cb[a + 1] ? -1.0 : 0.0);
+        if (sg == 0.0) continue;
+        const int vo = M.joints[a].vo;
+        for (int col = 0; col < dim[a]; ++col) {
+          const SV& s = S[a][col];
+          const V3 pv = s.lin + cross(s.ang, c.p);  // [−[r]×, I] (ω; v)
+          Jm[(size_t)(3 * k) * nv + vo + col] = sg * dot(c.n, pv);
+          Jm[(size_t)(3 * k + 1) * nv + vo + col] = sg * dot(tt, pv);
+          Jm[(size_t)(3 * k + 2) * nv + vo + col] = sg * dot(bb, pv);
+        }
+      }
+    }
+    // G = J M⁻¹ Jᵀ (M⁻¹ by LU, column by column), g = J v_free
+    std::vector<double> Minv((size_t)nv * nv);
+    for (int j = 0; j < nv; ++j) {
+      std::vector<double> e(nv, 0.0);
+      e[j] = 1.0;
+      if (!lu_solve(w.M, nv, e)) return GPB_ST_CHOL_FAIL;
+      for (int i = 0; i < nv; ++i) Minv[(size_t)i * nv + j] = e[i];
+    }
+    std::vector<double> JMi((size_t)m * nv, 0.0), G((size_t)m * m, 0.0), g(m, 0.0), lam(m, 0.0);
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < nv; ++j) {
+        double s2 = 0.0;
+        for (int k = 0; k < nv; ++k) s2 += Jm[(size_t)i * nv + k] * Minv[(size_t)k * nv + j];
+        JMi[(size_t)i * nv + j] = s2;
+      }
+    for (int i = 0; i < m; ++i) {
+      for (int j = 0; j < m; ++j) {
+        double s2 = 0.0;
+        for (int k = 0; k < nv; ++k) s2 += JMi[(size_t)i * nv + k] * Jm[(size_t)j * nv + k];
+        G[(size_t)i * m + j] = s2;
+      }
+      double s3 = 0.0;
+      for (int k = 0; k < nv; ++k) s3 += Jm[(size_t)i * nv + k] * vf[k];
+      g[i] = s3;
+    }
+    orc_socp::Info si;
+    const int r = orc_socp::solve(nc, G.data(), g.data(), 0.95, lam.data(), &si);
+    if (info) info[1] = si.iterations;
+    for (double x : lam)
+      if (std::isnan(x) || r != 0) return GPB_ST_SOLVER;
+    std::vector<double> imp(nv, 0.0);  // Jᵀ λ
+    for (int i = 0; i < m; ++i)
+      for (int k = 0; k < nv; ++k) imp[k] += Jm[(size_t)i * nv + k] * lam[i];
+    if (!lu_solve(w.M, nv, imp)) return GPB_ST_CHOL_FAIL;
+    for (int i = 0; i < nv; ++i) vn[i] = vf[i] + imp[i];
+    if (det) {
+      det->J = Jm;
+      det->lambda = lam;
+      det->iterations = si.iterations;
+    }
+  }
+  if (det) {
+    det->nc = nc;
+    det->Mm = w.M;
+    det->vfree = vf;
+    det->vnext = vn;
+  }
+  // compute_new_q with the new velocity (src/integrators.rs:296-319)
+  for (const Joint& J : M.joints) {
+    if (J.type == GPB_JOINT_REVOLUTE || J.type == GPB_JOINT_PRISMATIC) {
+      q[J.qo] = q[J.qo] + vn[J.vo] * dt;
+    } else if (J.type == GPB_JOINT_FLOATING) {
+      double qn[7];
+      pose_advance(q + J.qo, vn.data() + J.vo, dt, qn);
+      for (int k = 0; k < 7; ++k) q[J.qo + k] = qn[k];
+    }
+  }
+  for (int i = 0; i < nv; ++i) v[i] = vn[i];
+  for (int i = 0; i < M.nq; ++i)
+    if (!std::isfinite(q[i])) return GPB_ST_NONFINITE;
+  return 0;
+}
+
 // One step (src/simulate.rs:20-83) in place.
 static int step(const Mechanism& M, double* q, double* v, const double* tau, double dt,
                 int integrator, int solver, Work& w) {
   int nq = M.nq, nv = M.nv;
+  if (integrator == GPB_VELOCITY_STEPPING) return velocity_step(M, q, v, tau, dt, w, nullptr);
   std::vector<double> qn(q, q + nq), vn(v, v + nv), f1(nv), f2(nv), f3(nv), f4(nv);
   int st = 0;
   if (integrator == GPB_SEMI_IMPLICIT_EULER) {
@@ -982,6 +1175,40 @@ int oracle_collide_cuboids(int64_t n, const double* pose_a, const double* dims_a
     }
   }
   return 0;
+}
+
+// One velocity-stepping step of instance `inst` with its program: returns the
+// status; *nc, and (each sized for max_contacts contacts) J (3nc × nv,
+// row-major), M (nv × nv), v_free, λ (3nc), v_next; q, v advanced in place.
+int oracle_vs_step(const gpb_model* m, int64_t inst, double* q, double* v, const double* tau, double dt,
+                   int max_contacts, int32_t* nc, double* J, double* Mm, double* vfree, double* lambda,
+                   double* vnext) {
+  orc::Mechanism M;
+  if (!orc::load_mechanism(m, inst, M)) return GPB_E_INVAL;
+  orc::Work w;
+  orc::VSDetails d;
+  const int st = orc::velocity_step(M, q, v, tau, dt, w, nullptr, &d);
+  *nc = d.nc;
+  if (d.nc > max_contacts) return GPB_E_RANGE;
+  std::copy(d.J.begin(), d.J.end(), J);
+  std::copy(d.Mm.begin(), d.Mm.end(), Mm);
+  std::copy(d.vfree.begin(), d.vfree.end(), vfree);
+  std::copy(d.lambda.begin(), d.lambda.end(), lambda);
+  std::copy(d.vnext.begin(), d.vnext.end(), vnext);
+  return st;
+}
+
+// The velocity-stepping friction-cone program on its own (socp.h): nc contacts,
+// G row-major (3nc)², g (3nc); info = iterations, residual, gap.
+int oracle_socp_solve(int nc, const double* G, const double* g, double mu, double* lambda, double* info) {
+  orc_socp::Info in;
+  const int r = orc_socp::solve(nc, G, g, mu, lambda, &in);
+  if (info) {
+    info[0] = in.iterations;
+    info[1] = in.residual;
+    info[2] = in.gap;
+  }
+  return r;
 }
 
 // Articulated::free_velocity (src/hybrid/articulated/mod.rs:124-199,
