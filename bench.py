@@ -66,6 +66,8 @@ def parse():
                     help="cuboid-collider workload: build_gripper batches (GJK/EPA jaw-cube "
                          "contacts) and independent collision queries")
     ap.add_argument("--pairs", type=int, default=1 << 22, help="collision queries per timed launch")
+    ap.add_argument("--vstep", action="store_true",
+                    help="velocity stepping (friction-cone impulses) on cubes resting on the ground")
     return ap.parse_args()
 
 
@@ -803,6 +805,104 @@ def cpu_cuboids(M, q0, v0, steps, seconds_target=12.0):
             "sample": f"first {sample} of {M.n} grippers x {K} steps (oracle restatement, {threads} host threads)"}
 
 
+# ---------------------------------------------------------------------------
+# velocity stepping: the floating-cube configuration's cubes placed resting on
+# the ground (1-4 corners in contact), one friction-cone program per cube-step
+
+VSTEP_DT = 1e-3
+
+
+def resting_cubes(n, seed):
+    from gpb import Model, builders
+
+    M, _, _, _ = Model.from_config(2, n, seed=seed)
+    side = 2.0 * np.abs(M.contact_params.reshape(-1, 6)[::8, 0])  # first corner: (l/2, l/2, -l/2)
+    q, v = builders.resting_cube_states(np.random.default_rng(seed), M, lambda i: side[i], tilt=0.005)
+    return M, q, v
+
+
+def run_vstep(args):
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import gpb
+    from gpb import Batch
+
+    L = gpb.lib()
+    ctx = gpb.Context(local)
+    n = args.instances
+    M, q0, v0 = resting_cubes(n, shard_seed(args.seed, rank))
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    w, _ = B.autotune(VSTEP_DT, gpb.VELOCITY_STEPPING, gpb.FP64, trial_steps=5)
+    if args.warmup:
+        B.simulate_steps(args.warmup, VSTEP_DT, gpb.VELOCITY_STEPPING)
+    ctx.synchronize()
+    with Clocks(local) as clk:
+        l0 = ctx.launches
+        B.simulate_steps(args.steps, VSTEP_DT, gpb.VELOCITY_STEPPING, step0=args.warmup)
+        kernel_ms = L.gpb_last_launch_ms(ctx.h)
+        ctx.synchronize()
+        launches = ctx.launches - l0
+    kernel_ms = all_reduce(kernel_ms, "max", world, f"cuda:{local}")
+    done = all_reduce(float(B.steps_done().sum()), "sum", world, f"cuda:{local}")
+    failed = int(np.sum(B.status() != 0))
+    # e2e: pinned host state in, K steps, state out
+    q_h = torch.from_numpy(q0).pin_memory().numpy()
+    v_h = torch.from_numpy(v0).pin_memory().numpy()
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    B.update(q_h, v_h)
+    B.clear_status()
+    B.simulate_steps(args.steps, VSTEP_DT, gpb.VELOCITY_STEPPING)
+    qo, vo = B.state()
+    e2e_s = all_reduce(time.perf_counter() - t0, "max", world, f"cuda:{local}")
+    e2e_done = all_reduce(float(B.steps_done().sum()), "sum", world, f"cuda:{local}")
+    line = {
+        "metric": "instance-steps/s of velocity stepping (friction-cone impulse program per step)",
+        "value": done / (kernel_ms * 1e-3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": kernel_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (the floating-cube configuration's cubes, seeded resting states)",
+        "config": {"workload": f"resting cube x {n} per GPU (8 corner contacts, ground plane)",
+                   "dt": VSTEP_DT, "integrator": "velocity stepping", "warps_per_sm": w,
+                   "l2": "inputs larger than L2 (topology + state + scratch > 129 MB)"},
+        "gpu_launches": launches, "clocks": clk.summary(), "failed_instances": failed,
+        "e2e": {"value": e2e_done / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (q_h.nbytes + v_h.nbytes) / args.steps,
+                "d2h_bytes_per_step": (qo.nbytes + vo.nbytes) / args.steps,
+                "note": "gpb_set_state (pinned host) + gpb_simulate + gpb_get_state"},
+    }
+    if rank == 0 and not args.skip_cpu:
+        import oracle
+
+        threads = os.cpu_count() or 1
+        qc, vc = q0.copy(), v0.copy()
+        cal = min(n, 8 * threads)
+        t = time.perf_counter()
+        oracle.simulate_batch(M, qc, vc, VSTEP_DT, 2, integrator=gpb.VELOCITY_STEPPING, end=cal, threads=threads)
+        per = (time.perf_counter() - t) / (cal * 2)
+        sample = min(n, 4096)
+        K = max(5, min(args.steps, int(12.0 / max(per * sample, 1e-9))))
+        qc, vc = q0.copy(), v0.copy()
+        t = time.perf_counter()
+        oracle.simulate_batch(M, qc, vc, VSTEP_DT, K, integrator=gpb.VELOCITY_STEPPING, end=sample,
+                              threads=threads)
+        el = time.perf_counter() - t
+        line["cpu_baseline"] = {"value": sample * K / el, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"first {sample} of {n} cubes x {K} steps (oracle restatement, "
+                                          f"{threads} host threads)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -811,6 +911,8 @@ def main():
         return run_serve(args)
     if args.cuboids:
         return run_cuboids(args)
+    if args.vstep:
+        return run_vstep(args)
     return run_gpu(args)
 
 

@@ -179,3 +179,24 @@ def cuboid_pairs(rng, n: int, kind: str = "shallow"):
         qb /= np.linalg.norm(qb, axis=1)[:, None]
         return np.concatenate([qa, c], 1), da, np.concatenate([qb, bc], 1), db
     raise ValueError(f"unknown pair distribution {kind!r}")
+
+
+def resting_cube_states(rng, model, scale_of, tilt: float = 0.2, depth: float = 2e-3):
+    """States of one-cube mechanisms (a FloatingJoint with its 8 corner contacts
+    on the ground z ≥ 0) resting near the ground: tilted by up to `tilt` rad,
+    the lowest corner 0-`depth` m below the plane, v ~ N(0, 0.5²).  `scale_of(i)`
+    is instance i's side length.  Returns flat (q, v)."""
+    n = model.n
+    q = np.zeros((n, 7))
+    q[:, :4] = _euler_quats(rng, n, tilt)
+    corners = np.array([[sx, sy, sz] for sx in (-.5, .5) for sy in (-.5, .5) for sz in (-.5, .5)])
+    for i in range(n):
+        x, y, z, w = q[i, :4]
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        zc = (corners * scale_of(i)) @ R[2]
+        q[i, 4:6] = rng.uniform(-1.0, 1.0, 2)
+        q[i, 6] = -zc.min() - rng.uniform(0.0, depth)
+    v = rng.normal(0.0, 0.5, (n, 6))
+    return q.ravel(), v.ravel()

@@ -956,6 +956,12 @@ static int velocity_step(const Mechanism& M, double* q, double* v, const double*
       for (int k = 0; k < nv; ++k) s3 += Jm[(size_t)i * nv + k] * vf[k];
       g[i] = s3;
     }
+    if (det) {  // the program, also when it fails
+      det->nc = nc;
+      det->J = Jm;
+      det->Mm = w.M;
+      det->vfree = vf;
+    }
     orc_socp::Info si;
     const int r = orc_socp::solve(nc, G.data(), g.data(), 0.95, lam.data(), &si);
     if (info) info[1] = si.iterations;
@@ -1190,6 +1196,8 @@ int oracle_vs_step(const gpb_model* m, int64_t inst, double* q, double* v, const
   const int st = orc::velocity_step(M, q, v, tau, dt, w, nullptr, &d);
   *nc = d.nc;
   if (d.nc > max_contacts) return GPB_E_RANGE;
+  d.lambda.resize(3 * (size_t)d.nc);
+  d.vnext.resize(d.vfree.size());
   std::copy(d.J.begin(), d.J.end(), J);
   std::copy(d.Mm.begin(), d.Mm.end(), Mm);
   std::copy(d.vfree.begin(), d.vfree.end(), vfree);

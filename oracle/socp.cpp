@@ -175,14 +175,15 @@ int solve(int nc, const double* G, const double* g, double mu, double* lambda, I
       gap += y[i] * z[i];
       obj += y[i] * (q[i] + 0.5 * (r[i] + z[i] - q[i]));
     }
-    // stop at 1e-10 relative (Clarabel's defaults are 1e-8); when the Newton
-    // matrix loses definiteness at the end of the path, accept 1e-8
+    // stop at a dual residual of 1e-9 and a gap of 1e-10 (relative); when the
+    // Newton matrix loses definiteness at the end of the path, or the
+    // iterations run out, accept 1e-7 / 1e-8 (Clarabel's defaults are 1e-8)
     const double scale = 1.0 + std::max(qn, std::fabs(obj));
-    if (rn <= 1e-10 * (1.0 + qn) && gap <= 1e-10 * scale) {
+    if (rn <= 1e-9 * (1.0 + qn) && gap <= 1e-10 * scale) {
       status = 0;
       break;
     }
-    last_ok = rn <= 1e-8 * (1.0 + qn) && gap <= 1e-8 * scale;
+    last_ok = rn <= 1e-7 * (1.0 + qn) && gap <= 1e-8 * scale;
     for (int c = 0; c < nc; ++c) {
       nt_scaling(&y[3 * c], &z[3 * c], &S[c]);
       mul3(S[c].W, &z[3 * c], &lam[3 * c]);
@@ -232,6 +233,7 @@ int solve(int nc, const double* G, const double* g, double mu, double* lambda, I
       z[i] += alpha * dz[i];
     }
   }
+  if (status != 0 && last_ok) status = 0;  // out of iterations at reduced accuracy
   for (int i = 0; i < m; ++i) lambda[i] = D[i] * y[i];
   if (info) {
     info->iterations = it;
