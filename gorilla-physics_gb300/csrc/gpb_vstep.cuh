@@ -35,8 +35,8 @@ __device__ __forceinline__ double jdot(const double* u, const double* v) {
 
 // sup{α ≥ 0 : u + α d ∈ Q} for u strictly inside the Lorentz cone Q.
 __device__ __forceinline__ double max_step(const double* u, const double* d) {
-  if (d[0] >= sqrt(d[1] * d[1] + d[2] * d[2])) return 1e300;
   const double a = jdot(d, d), b = jdot(u, d), c = jdot(u, u);
+  if (d[0] >= 0.0 && a >= 0.0) return 1e300;  // d ∈ Q: the ray never leaves
   if (a == 0.0) return b < 0.0 ? -c / (2.0 * b) : 1e300;
   const double disc = b * b - a * c;
   if (disc < 0.0) return 1e300;
@@ -51,18 +51,22 @@ __device__ __forceinline__ double max_step(const double* u, const double* d) {
 // Nesterov–Todd scaling of one cone pair (s, z): W = η(2vvᵀ − J),
 // W⁻¹ = (2JvvᵀJ − J)/η with v built from the normalised scaling point.
 __device__ __forceinline__ void nt_scaling(const double* s, const double* z, double* W, double* Wi, double* eta) {
-  const double sn = sqrt(jdot(s, s)), zn = sqrt(jdot(z, z));
+  // reciprocal square roots and one division per reciprocal, multiplications
+  // elsewhere (FP64 division and square root are multi-instruction sequences
+  // on the FP64 unit; the solver needs no correctly rounded results)
+  const double rsn = rsqrt(jdot(s, s)), rzn = rsqrt(jdot(z, z));
+  const double sn = jdot(s, s) * rsn;
   double sb[3], zb[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    sb[k] = s[k] / sn;
-    zb[k] = z[k] / zn;
+    sb[k] = s[k] * rsn;
+    zb[k] = z[k] * rzn;
   }
-  const double g2 = 2.0 * sqrt((1.0 + sb[0] * zb[0] + sb[1] * zb[1] + sb[2] * zb[2]) / 2.0);
-  const double w0 = (sb[0] + zb[0]) / g2, w1 = (sb[1] - zb[1]) / g2, w2 = (sb[2] - zb[2]) / g2;
-  const double nv = sqrt(2.0 * (w0 + 1.0));
-  const double v[3] = {(w0 + 1.0) / nv, w1 / nv, w2 / nv};
-  const double e = sqrt(sn / zn);
+  const double rg2 = 0.5 * rsqrt((1.0 + sb[0] * zb[0] + sb[1] * zb[1] + sb[2] * zb[2]) * 0.5);
+  const double w0 = (sb[0] + zb[0]) * rg2, w1 = (sb[1] - zb[1]) * rg2, w2 = (sb[2] - zb[2]) * rg2;
+  const double rnv = rsqrt(2.0 * (w0 + 1.0));
+  const double v[3] = {(w0 + 1.0) * rnv, w1 * rnv, w2 * rnv};
+  const double e = sqrt(sn * rzn), re = 1.0 / e;
   const double J[3] = {1.0, -1.0, -1.0};
 #pragma unroll
   for (int i = 0; i < 3; ++i)
@@ -70,7 +74,7 @@ __device__ __forceinline__ void nt_scaling(const double* s, const double* z, dou
     for (int j = 0; j < 3; ++j) {
       const double jij = i == j ? J[i] : 0.0;
       W[3 * i + j] = e * (2.0 * v[i] * v[j] - jij);
-      Wi[3 * i + j] = (2.0 * J[i] * v[i] * v[j] * J[j] - jij) / e;
+      Wi[3 * i + j] = (2.0 * J[i] * v[i] * v[j] * J[j] - jij) * re;
     }
   *eta = e;
 }
@@ -81,15 +85,15 @@ __device__ __forceinline__ void jprod(const double* u, const double* v, double* 
   o[2] = u[0] * v[2] + v[0] * u[2];
 }
 
-// In-place Cholesky of the m × m matrix at H (lower triangle); false if not SPD.
+// In-place Cholesky of the m × m matrix at H (lower triangle, the diagonal
+// stored as 1 / L_ii); false if not SPD.
 __device__ __forceinline__ bool chol(const View& V, int H, int m) {
   for (int j = 0; j < m; ++j) {
     double d = V(H + j * m + j);
     for (int k = 0; k < j; ++k) d -= V(H + j * m + k) * V(H + j * m + k);
     if (!(d > 0.0)) return false;
-    d = sqrt(d);
-    V(H + j * m + j) = d;
-    const double di = 1.0 / d;
+    const double di = rsqrt(d);
+    V(H + j * m + j) = di;  // the reciprocal: solves multiply
     for (int i = j + 1; i < m; ++i) {
       double s = V(H + i * m + j);
       for (int k = 0; k < j; ++k) s -= V(H + i * m + k) * V(H + j * m + k);
@@ -98,16 +102,17 @@ __device__ __forceinline__ bool chol(const View& V, int H, int m) {
   }
   return true;
 }
+// Solve with the factor of chol(), whose diagonal holds 1 / L_ii.
 __device__ __forceinline__ void chol_solve(const View& V, int H, int m, int x) {
   for (int i = 0; i < m; ++i) {
     double s = V(x + i);
     for (int k = 0; k < i; ++k) s -= V(H + i * m + k) * V(x + k);
-    V(x + i) = s / V(H + i * m + i);
+    V(x + i) = s * V(H + i * m + i);
   }
   for (int i = m - 1; i >= 0; --i) {
     double s = V(x + i);
     for (int k = i + 1; k < m; ++k) s -= V(H + k * m + i) * V(x + k);
-    V(x + i) = s / V(H + i * m + i);
+    V(x + i) = s * V(H + i * m + i);
   }
 }
 
@@ -124,10 +129,10 @@ __device__ __forceinline__ void newton(const View& V, const VSLayout& L, int nc,
       l[k] = V(L.lam + 3 * c + k);
       d[k] = V(L.ds + 3 * c + k);
     }
-    const double det = jdot(l, l);
-    x[0] = (l[0] * d[0] - l[1] * d[1] - l[2] * d[2]) / det;
-    x[1] = (d[1] - x[0] * l[1]) / l[0];
-    x[2] = (d[2] - x[0] * l[2]) / l[0];
+    const double rdet = 1.0 / jdot(l, l), rl0 = 1.0 / l[0];
+    x[0] = (l[0] * d[0] - l[1] * d[1] - l[2] * d[2]) * rdet;
+    x[1] = (d[1] - x[0] * l[1]) * rl0;
+    x[2] = (d[2] - x[0] * l[2]) * rl0;
 #pragma unroll
     for (int k = 0; k < 3; ++k) V(L.rs + 3 * c + k) = x[k];
 #pragma unroll
