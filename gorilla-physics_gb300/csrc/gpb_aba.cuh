@@ -316,18 +316,30 @@ __device__ __forceinline__ SV<R> abi_mul_r(const ABI& I, const SV<R>& x) {
 }
 
 // (Rrel, t) of body b in the sweep precision: the FP64 record in the I
-// region, or (R = float) its FP32 copy in RF.
+// region, or (R = float) its FP32 copy in RF.  A planar rotation about e_k
+// (planar = k ≥ 0) is stored as (cos, sin) and rebuilt exactly.
 template <typename R>
-__device__ __forceinline__ void load_xf(const LaneCtx<R>& c, int b, M3<R>& Rr, V3<R>& t) {
-  if (sizeof(R) == 8) {
+__device__ __forceinline__ void load_xf(const LaneCtx<R>& c, int b, int planar, M3<R>& Rr, V3<R>& t) {
+  const int base = sizeof(R) == 8 ? c.L.I + 12 * b : c.L.RF + 12 * b;
+  auto at = [&](int e) -> R { return sizeof(R) == 8 ? R(c.d(base + e)) : c.r(base + e); };
+  if (planar >= 0) {
+    const int i1 = (planar + 1) % 3, i2 = (planar + 2) % 3;
+    const R co = at(0), si = at(1);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Rr.a[k] = R(c.d(c.L.I + 12 * b + k));
-    t = {R(c.d(c.L.I + 12 * b + 9)), R(c.d(c.L.I + 12 * b + 10)), R(c.d(c.L.I + 12 * b + 11))};
+    for (int e = 0; e < 9; ++e) Rr.a[e] = (e % 4 == 0) ? R(1) : R(0);
+    Rr.a[3 * i1 + i1] = co;
+    Rr.a[3 * i1 + i2] = -si;
+    Rr.a[3 * i2 + i1] = si;
+    Rr.a[3 * i2 + i2] = co;
   } else {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Rr.a[k] = c.r(c.L.RF + 12 * b + k);
-    t = {c.r(c.L.RF + 12 * b + 9), c.r(c.L.RF + 12 * b + 10), c.r(c.L.RF + 12 * b + 11)};
+    for (int k = 0; k < 9; ++k) Rr.a[k] = at(k);
   }
+  t = {at(9), at(10), at(11)};
+}
+// planar axis index of body b's joint (−1: not a planar rotation).
+__device__ __forceinline__ int planar_axis(int type, uint32_t fl) {
+  return (type == 1 && (fl & BF_INIT_ROT_IDENTITY) && (fl & BF_AXIS_PRINCIPAL)) ? (int)bf_axis_index(fl) : -1;
 }
 
 template <typename R>
@@ -570,15 +582,29 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         store_cuboid(c, uslot - 1, b, Rw, posw, omw, mul(Rw, vld) - cross(omw, posw));
       }
     }
-    // records for the inward and second outward passes
+    // records for the inward and second outward passes: (Rrel, t); a planar
+    // rotation keeps only its (cos, sin) — the other entries are 0 and 1 — so
+    // the passes that read it back touch 5 rows instead of 12
+    if (planar) {
+      const int k = (int)bf_axis_index(fl), i1 = (k + 1) % 3, i2 = (k + 2) % 3;
+      c.d(c.L.I + 12 * b) = Rd.a[3 * i1 + i1];
+      c.d(c.L.I + 12 * b + 1) = Rd.a[3 * i2 + i1];
+    } else {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) c.d(c.L.I + 12 * b + k) = Rd.a[k];
+      for (int k = 0; k < 9; ++k) c.d(c.L.I + 12 * b + k) = Rd.a[k];
+    }
     c.d(c.L.I + 12 * b + 9) = td.x;
     c.d(c.L.I + 12 * b + 10) = td.y;
     c.d(c.L.I + 12 * b + 11) = td.z;
     if (sizeof(R) == 4) {
+      if (planar) {
+        const int k = (int)bf_axis_index(fl), i1 = (k + 1) % 3, i2 = (k + 2) % 3;
+        c.r(c.L.RF + 12 * b) = Rr.a[3 * i1 + i1];
+        c.r(c.L.RF + 12 * b + 1) = Rr.a[3 * i2 + i1];
+      } else {
 #pragma unroll
-      for (int k = 0; k < 9; ++k) c.r(c.L.RF + 12 * b + k) = Rr.a[k];
+        for (int k = 0; k < 9; ++k) c.r(c.L.RF + 12 * b + k) = Rr.a[k];
+      }
       c.r(c.L.RF + 12 * b + 9) = t.x;
       c.r(c.L.RF + 12 * b + 10) = t.y;
       c.r(c.L.RF + 12 * b + 11) = t.z;
@@ -735,16 +761,17 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       const int pb = parent - 1;
       if (type != 3) {
         double Rr[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Rr[k] = c.d(c.L.I + 12 * b + k);
         const VD t{c.d(c.L.I + 12 * b + 9), c.d(c.L.I + 12 * b + 10), c.d(c.L.I + 12 * b + 11)};
-        int planar = -1;
+        const int planar = planar_axis(type, fl);
         double co = 1.0, si = 0.0;
-        if (type == 1 && (fl & BF_INIT_ROT_IDENTITY) && (fl & BF_AXIS_PRINCIPAL)) {
-          planar = (int)bf_axis_index(fl);
-          const int i1 = (planar + 1) % 3, i2 = (planar + 2) % 3;
-          co = Rr[3 * i1 + i1];
-          si = Rr[3 * i2 + i1];
+        if (planar >= 0) {  // (cos, sin) record; abi_to_parent does not read Rr then
+          co = c.d(c.L.I + 12 * b);
+          si = c.d(c.L.I + 12 * b + 1);
+#pragma unroll
+          for (int k = 0; k < 9; ++k) Rr[k] = 0.0;
+        } else {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) Rr[k] = c.d(c.L.I + 12 * b + k);
         }
         const ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si);
         if (pb == b - 1) {
@@ -760,7 +787,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       // force to the parent frame: (Rr n + t × Rr f, Rr f)
       M3<R> RrR;
       V tr;
-      load_xf(c, b, RrR, tr);
+      load_xf(c, b, planar_axis(type, fl), RrR, tr);
       const SV<R> fp = force_to_parent(RrR, tr, pa);
       if (pb == b - 1) {
         carryP = fp;
@@ -790,7 +817,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     }
     M3<R> Rr;
     V t;
-    load_xf(c, b, Rr, t);
+    load_xf(c, b, planar_axis(type, w1 & 255), Rr, t);
     // a' = X a_p + c
     a.v = mulT(Rr, a.v + cross(a.w, t));
     a.w = mulT(Rr, a.w);
