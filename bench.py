@@ -863,6 +863,22 @@ def run_vstep(args):
     qo, vo = B.state()
     e2e_s = all_reduce(time.perf_counter() - t0, "max", world, f"cuda:{local}")
     e2e_done = all_reduce(float(B.steps_done().sum()), "sum", world, f"cuda:{local}")
+    # FP64 roofline: executed FP64 operations per instance-step (ncu thread-level
+    # counters of predicated-on lanes, 2 per FMA) from the committed capture
+    import ctypes
+
+    tpk = ctypes.c_double()
+    gpb._abi.check(L.gpb_fma_peak(local, gpb.FP64, 32, ctypes.byref(tpk)), "gpb_fma_peak")
+    roof = None
+    try:
+        wk = json.loads((ROOT / "profiles" / "vstep_work.json").read_text())
+        ach = done / (kernel_ms * 1e-3) * wk["fp64_flops_per_instance_step"] / 1e12
+        roof = {"bound": "fp64", "achieved": ach, "peak": tpk.value, "unit": "TFLOP/s", "frac": ach / tpk.value,
+                "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (gpb_fma_peak), this run",
+                "work": f"{wk['fp64_flops_per_instance_step']:.0f} FP64 operations per instance-step "
+                        f"({wk['source']})"}
+    except (OSError, ValueError, KeyError):
+        pass
     line = {
         "metric": "instance-steps/s of velocity stepping (friction-cone impulse program per step)",
         "value": done / (kernel_ms * 1e-3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -872,7 +888,7 @@ def run_vstep(args):
         "config": {"workload": f"resting cube x {n} per GPU (8 corner contacts, ground plane)",
                    "dt": VSTEP_DT, "integrator": "velocity stepping", "warps_per_sm": w,
                    "l2": "inputs larger than L2 (topology + state + scratch > 129 MB)"},
-        "gpu_launches": launches, "clocks": clk.summary(), "failed_instances": failed,
+        "gpu_launches": launches, "clocks": clk.summary(), "failed_instances": failed, "roofline": roof,
         "e2e": {"value": e2e_done / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (q_h.nbytes + v_h.nbytes) / args.steps,
                 "d2h_bytes_per_step": (qo.nbytes + vo.nbytes) / args.steps,
                 "note": "gpb_set_state (pinned host) + gpb_simulate + gpb_get_state"},
