@@ -11,11 +11,17 @@
 // Precision: kinematics, bias forces and the final accelerations run in R
 // (double for GPB_FP64, float for GPB_MIXED).  The articulated inertias, the
 // projections U = I^A S, D = Sᵀ U and the congruence X*ᵀ I^a X to the parent
-// frame always run in FP64: that recursion subtracts U D⁻¹ Uᵀ from I^A and is
+// frame need more than FP32: that recursion subtracts U D⁻¹ Uᵀ from I^A and is
 // where FP32 loses digits on long chains (FP32 everywhere gives q̈ errors up to
-// 2e-5 of |q̈| on 48-DOF chains; FP64 here keeps them below 1e-5).  The poses
-// that place contact points are computed in FP64 whenever an instance has
-// contacts (a penetration error ε·|p| becomes a force error k·ε·|p|).
+// 2e-5 of |q̈| on 48-DOF chains).  GPB_FP64 runs it in FP64; GPB_MIXED runs it
+// in double-float (gpb_ff.cuh, about 48 bits) on the FP32 pipes, from the
+// FP32-rounded model and the FP32 joint transforms of its kinematics — the
+// exact recursion of a model perturbed by ≤ 6e-8 relative, which moves q̈ of
+// the 48-DOF chains by less than 1e-6 of max |q̈|.  The q̈ solve of a 1-DOF
+// joint, D⁻¹ (u − Uᵀ a), is double-float too; a floating joint's 6×6 solve
+// stays FP64.  The poses that place contact points are computed in FP64
+// whenever an instance has contacts (a penetration error ε·|p| becomes a force
+// error k·ε·|p|).
 #pragma once
 
 // Symmetric 6×6 spatial inertia in blocks [[A, B], [Bᵀ, C]] acting on (ω, v):
@@ -26,7 +32,8 @@ struct ABI {
 };
 constexpr int ABI_D = 21;
 
-__device__ __forceinline__ double symget(const double* S, int i, int j) {
+template <typename T>
+__device__ __forceinline__ T symget(const T* S, int i, int j) {
   // (0,0)=0 (1,1)=1 (2,2)=2 (0,1)=3 (0,2)=4 (1,2)=5
   if (i == j) return S[i];
   const int a = i < j ? i : j, b = i < j ? j : i;
@@ -116,51 +123,114 @@ __device__ __forceinline__ void gen_rotate(const double* R, const double* B, dou
       out[3 * i + j] = P[3 * i] * R[3 * j] + P[3 * i + 1] * R[3 * j + 1] + P[3 * i + 2] * R[3 * j + 2];
 }
 
-// Rotation about principal axis k by (cos, sin), applied to the rows of a
-// 3-column block (x_i1' = c x_i1 − s x_i2, x_i2' = s x_i1 + c x_i2 with
-// i1 = k+1, i2 = k+2 mod 3) or to its columns.
-__device__ __forceinline__ void planar_rows(double* M, int k, double co, double si) {
-  const int i1 = (k + 1) % 3, i2 = (k + 2) % 3;
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const double a = M[3 * i1 + j], b = M[3 * i2 + j];
-    M[3 * i1 + j] = co * a - si * b;
-    M[3 * i2 + j] = si * a + co * b;
-  }
+// Three-way choice by a runtime axis index, written as selects: a small array
+// indexed by a runtime value would be placed in local memory.
+template <typename T>
+__device__ __forceinline__ T pick3(int k, T x0, T x1, T x2) {
+  return k == 0 ? x0 : (k == 1 ? x1 : x2);
 }
-__device__ __forceinline__ void planar_cols(double* M, int k, double co, double si) {
-  const int i1 = (k + 1) % 3, i2 = (k + 2) % 3;
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    const double a = M[3 * r + i1], b = M[3 * r + i2];
-    M[3 * r + i1] = co * a - si * b;
-    M[3 * r + i2] = si * a + co * b;
-  }
-}
-// R S Rᵀ for symmetric S (packed) and the rotation about principal axis k:
-// only the (i1, i2) plane mixes.
-__device__ __forceinline__ void sym_planar(double* S, int k, double co, double si) {
-  const int i1 = (k + 1) % 3, i2 = (k + 2) % 3;
-  // packed index of (i, j)
-  auto pk = [](int i, int j) { return i == j ? i : ((i + j == 1) ? 3 : ((i + j == 2) ? 4 : 5)); };
-  const double a = S[pk(i1, i1)], b = S[pk(i2, i2)], d = S[pk(i1, i2)];
-  const double e1 = S[pk(i1, k)], e2 = S[pk(i2, k)];
-  const double c2 = co * co, s2 = si * si, cs = co * si;
-  const double cs2d = 2.0 * cs * d;
-  S[pk(i1, i1)] = c2 * a + s2 * b - cs2d;
-  S[pk(i2, i2)] = s2 * a + c2 * b + cs2d;
-  S[pk(i1, i2)] = cs * (a - b) + (c2 - s2) * d;
-  S[pk(i1, k)] = co * e1 - si * e2;
-  S[pk(i2, k)] = si * e1 + co * e2;
+// Rotation about principal axis e_k by (cos, sin): only the (k+1, k+2) plane
+// (mod 3) turns.
+template <typename T>
+__device__ __forceinline__ M3<T> planar_rot(int k, T co, T si) {
+  const T z = T(0), o = T(1);
+  M3<T> R;
+  R.a[0] = k == 0 ? o : co;
+  R.a[1] = k == 2 ? -si : z;
+  R.a[2] = k == 1 ? si : z;
+  R.a[3] = k == 2 ? si : z;
+  R.a[4] = k == 1 ? o : co;
+  R.a[5] = k == 0 ? -si : z;
+  R.a[6] = k == 1 ? -si : z;
+  R.a[7] = k == 0 ? si : z;
+  R.a[8] = k == 2 ? o : co;
+  return R;
 }
 
-__device__ __forceinline__ void sym_expand(const double* S, double* F) {
+// One plane rotation of a pair: (co·a − si·b, si·a + co·b), in FP64 or in
+// double-float with FP32 (cos, sin).
+__device__ __forceinline__ void rot2(double a, double b, double co, double si, double& x, double& y) {
+  x = co * a - si * b;
+  y = si * a + co * b;
+}
+__device__ __forceinline__ void rot2(FF a, FF b, float co, float si, FF& x, FF& y) {
+  x = ff_lin2(a, co, b, -si);
+  y = ff_lin2(a, si, b, co);
+}
+
+// The rotation about principal axis k applied to the rows of a 3-column block
+// (x_i1' = c x_i1 − s x_i2, x_i2' = s x_i1 + c x_i2 with i1 = k+1, i2 = k+2
+// mod 3) or to its columns.
+template <typename W, typename S>
+__device__ __forceinline__ void planar_rows(W* M, int k, S co, S si) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    W x, y;
+    rot2(pick3(k, M[3 + j], M[6 + j], M[j]), pick3(k, M[6 + j], M[j], M[3 + j]), co, si, x, y);
+    M[j] = pick3(k, M[j], y, x);
+    M[3 + j] = pick3(k, x, M[3 + j], y);
+    M[6 + j] = pick3(k, y, x, M[6 + j]);
+  }
+}
+template <typename W, typename S>
+__device__ __forceinline__ void planar_cols(W* M, int k, S co, S si) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    W x, y;
+    rot2(pick3(k, M[3 * r + 1], M[3 * r + 2], M[3 * r]), pick3(k, M[3 * r + 2], M[3 * r], M[3 * r + 1]), co, si,
+         x, y);
+    M[3 * r] = pick3(k, M[3 * r], y, x);
+    M[3 * r + 1] = pick3(k, x, M[3 * r + 1], y);
+    M[3 * r + 2] = pick3(k, y, x, M[3 * r + 2]);
+  }
+}
+// R S Rᵀ for symmetric S and the rotation about principal axis k: only the
+// plane block (a = S_i1i1, b = S_i2i2, d = S_i1i2) and the couplings to the
+// axis (e1 = S_i1k, e2 = S_i2k) change.
+__device__ __forceinline__ void sym_planar_terms(double a, double b, double d, double e1, double e2, double co,
+                                                 double si, double& a2, double& b2, double& d2, double& f1,
+                                                 double& f2) {
+  const double c2 = co * co, s2 = si * si, cs = co * si;
+  const double cs2d = 2.0 * cs * d;
+  a2 = c2 * a + s2 * b - cs2d;
+  b2 = s2 * a + c2 * b + cs2d;
+  d2 = cs * (a - b) + (c2 - s2) * d;
+  f1 = co * e1 - si * e2;
+  f2 = si * e1 + co * e2;
+}
+// double-float: rows, then columns (M = R S, S' = M Rᵀ), each entry one ff_lin2
+__device__ __forceinline__ void sym_planar_terms(FF a, FF b, FF d, FF e1, FF e2, float co, float si, FF& a2, FF& b2,
+                                                 FF& d2, FF& f1, FF& f2) {
+  FF m11, m21, m12, m22;
+  rot2(a, d, co, si, m11, m21);
+  rot2(d, b, co, si, m12, m22);
+  rot2(m11, m12, co, si, a2, d2);
+  b2 = ff_lin2(m21, si, m22, co);
+  rot2(e1, e2, co, si, f1, f2);
+}
+// packed order xx yy zz xy xz yz
+template <typename W, typename S>
+__device__ __forceinline__ void sym_planar(W* P, int k, S co, S si) {
+  W a2, b2, d2, f1, f2;
+  sym_planar_terms(pick3(k, P[1], P[2], P[0]), pick3(k, P[2], P[0], P[1]), pick3(k, P[5], P[4], P[3]),
+                   pick3(k, P[3], P[5], P[4]), pick3(k, P[4], P[3], P[5]), co, si, a2, b2, d2, f1, f2);
+  P[0] = pick3(k, P[0], b2, a2);
+  P[1] = pick3(k, a2, P[1], b2);
+  P[2] = pick3(k, b2, a2, P[2]);
+  P[3] = pick3(k, f1, f2, d2);
+  P[4] = pick3(k, f2, d2, f1);
+  P[5] = pick3(k, d2, f1, f2);
+}
+
+template <typename W>
+__device__ __forceinline__ void sym_expand(const W* S, W* F) {
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) F[3 * i + j] = symget(S, i, j);
 }
-__device__ __forceinline__ void sym_pack(const double* F, double* S) {
+template <typename W>
+__device__ __forceinline__ void sym_pack(const W* F, W* S) {
   S[0] = F[0], S[1] = F[4], S[2] = F[8], S[3] = F[1], S[4] = F[2], S[5] = F[5];
 }
 
@@ -230,6 +300,170 @@ __device__ __forceinline__ ABI abi_to_parent(const ABI& I, const double* Rr, V3<
   ABI o;
   shift_general(A, B, Cm, t, o);
   return o;
+}
+
+// ---- double-float articulated inertias (GPB_MIXED) -------------------------
+// The same blocks as ABI, each entry an FF pair; rotations and translations
+// are the FP32 joint transforms of the sweep.
+struct ABIF {
+  FF A[6], B[9], C[6];
+};
+
+// FF view of an 8-byte scratch word (the pair is stored as hi, lo).
+template <typename R>
+__device__ __forceinline__ FF& ffw(const LaneCtx<R>& c, int e) {
+  return *reinterpret_cast<FF*>(&c.d(e));
+}
+template <typename R>
+__device__ __forceinline__ void store_abi_ff(const LaneCtx<R>& c, int base, const ABIF& I) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) ffw(c, base + k) = I.A[k];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) ffw(c, base + 6 + k) = I.B[k];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) ffw(c, base + 15 + k) = I.C[k];
+}
+template <typename R>
+__device__ __forceinline__ ABIF load_abi_ff(const LaneCtx<R>& c, int base) {
+  ABIF I;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) I.A[k] = ffw(c, base + k);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) I.B[k] = ffw(c, base + 6 + k);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) I.C[k] = ffw(c, base + 15 + k);
+  return I;
+}
+__device__ __forceinline__ void abi_add(ABIF& a, const ABIF& b) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) a.A[k] = ff_add(a.A[k], b.A[k]);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) a.B[k] = ff_add(a.B[k], b.B[k]);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) a.C[k] = ff_add(a.C[k], b.C[k]);
+}
+__device__ __forceinline__ ABI abi_to_double(const ABIF& I) {
+  ABI o;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) o.A[k] = ff_to_double(I.A[k]);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) o.B[k] = ff_to_double(I.B[k]);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) o.C[k] = ff_to_double(I.C[k]);
+  return o;
+}
+// Rigid-body inertia from the FP32 topology table.
+template <typename R>
+__device__ __forceinline__ ABIF body_abi_ff(const LaneCtx<R>& c, int tb) {
+  ABIF I;
+  const float m = c.t(tb + TD_INERTIA);
+  const float cx = c.t(tb + TD_INERTIA + 1), cy = c.t(tb + TD_INERTIA + 2), cz = c.t(tb + TD_INERTIA + 3);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) I.A[k] = ff(c.t(tb + TD_INERTIA + 4 + k));
+  I.B[0] = ff(0.0f), I.B[1] = ff(-cz), I.B[2] = ff(cy);
+  I.B[3] = ff(cz), I.B[4] = ff(0.0f), I.B[5] = ff(-cx);
+  I.B[6] = ff(-cy), I.B[7] = ff(cx), I.B[8] = ff(0.0f);
+  I.C[0] = I.C[1] = I.C[2] = ff(m);
+  I.C[3] = I.C[4] = I.C[5] = ff(0.0f);
+  return I;
+}
+// S' = R S Rᵀ (S symmetric) and B' = R B Rᵀ for an FP32 rotation R.
+__device__ __forceinline__ void sym_rotate(const float* R, const FF* S, FF* out) {
+  FF P[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      P[3 * i + j] = ff_dot3f(symget(S, 0, j), symget(S, 1, j), symget(S, 2, j), R[3 * i], R[3 * i + 1], R[3 * i + 2]);
+  const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+    out[k] = ff_dot3f(P[3 * ii[k]], P[3 * ii[k] + 1], P[3 * ii[k] + 2], R[3 * jj[k]], R[3 * jj[k] + 1],
+                      R[3 * jj[k] + 2]);
+}
+__device__ __forceinline__ void gen_rotate(const float* R, const FF* B, FF* out) {
+  FF P[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      P[3 * i + j] = ff_dot3f(B[j], B[3 + j], B[6 + j], R[3 * i], R[3 * i + 1], R[3 * i + 2]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      out[3 * i + j] = ff_dot3f(P[3 * i], P[3 * i + 1], P[3 * i + 2], R[3 * j], R[3 * j + 1], R[3 * j + 2]);
+}
+// The shift of shift_general with an FP32 translation.
+__device__ __forceinline__ void shift_general(const FF* A, const FF* B, const FF* Cm, V3<float> t, ABIF& o) {
+  FF W[9], BT[9];  // W = T C', BT = B' T
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    W[j] = ff_lin2(Cm[3 + j], -t.z, Cm[6 + j], t.y);
+    W[3 + j] = ff_lin2(Cm[j], t.z, Cm[6 + j], -t.x);
+    W[6 + j] = ff_lin2(Cm[j], -t.y, Cm[3 + j], t.x);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    BT[3 * i] = ff_lin2(B[3 * i + 1], t.z, B[3 * i + 2], -t.y);
+    BT[3 * i + 1] = ff_lin2(B[3 * i], -t.z, B[3 * i + 2], t.x);
+    BT[3 * i + 2] = ff_lin2(B[3 * i], t.y, B[3 * i + 1], -t.x);
+  }
+  const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const int i = ii[k], j = jj[k];
+    const FF wt = j == 0 ? ff_lin2(W[3 * i + 1], t.z, W[3 * i + 2], -t.y)
+                         : (j == 1 ? ff_lin2(W[3 * i], -t.z, W[3 * i + 2], t.x)
+                                   : ff_lin2(W[3 * i], t.y, W[3 * i + 1], -t.x));
+    o.A[k] = ff_sub(A[3 * i + j], ff_add3(BT[3 * i + j], BT[3 * j + i], wt));
+    o.C[k] = Cm[3 * i + j];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) o.B[k] = ff_add(B[k], W[k]);
+}
+// abi_to_parent in double-float: the child's FP32 transform (Rr, t), or its
+// (co, si) about principal axis `planar`.
+__device__ __forceinline__ ABIF abi_to_parent(const ABIF& I, const M3<float>& Rr, V3<float> t, int planar, float co,
+                                              float si) {
+  FF A[9], B[9], Cm[9];
+  FF a6[6], c6[6];
+  if (planar >= 0) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      a6[k] = I.A[k];
+      c6[k] = I.C[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) B[k] = I.B[k];
+    sym_planar(a6, planar, co, si);
+    sym_planar(c6, planar, co, si);
+    planar_rows(B, planar, co, si);
+    planar_cols(B, planar, co, si);
+  } else {
+    sym_rotate(Rr.a, I.A, a6);
+    sym_rotate(Rr.a, I.C, c6);
+    gen_rotate(Rr.a, I.B, B);
+  }
+  sym_expand(a6, A);
+  sym_expand(c6, Cm);
+  ABIF o;
+  shift_general(A, B, Cm, t, o);
+  return o;
+}
+// I·(w, v) from the leading FP32 parts (the bias-force update needs only FP32).
+__device__ __forceinline__ SV<float> abi_mul_hi(const ABIF& I, const SV<float>& x) {
+  const float w[3] = {x.w.x, x.w.y, x.w.z}, v[3] = {x.v.x, x.v.y, x.v.z};
+  float ow[3], ov[3];
+  const int s[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    ow[i] = I.A[s[i][0]].hi * w[0] + I.A[s[i][1]].hi * w[1] + I.A[s[i][2]].hi * w[2] + I.B[3 * i].hi * v[0] +
+            I.B[3 * i + 1].hi * v[1] + I.B[3 * i + 2].hi * v[2];
+    ov[i] = I.B[i].hi * w[0] + I.B[3 + i].hi * w[1] + I.B[6 + i].hi * w[2] + I.C[s[i][0]].hi * v[0] +
+            I.C[s[i][1]].hi * v[1] + I.C[s[i][2]].hi * v[2];
+  }
+  return {{ow[0], ow[1], ow[2]}, {ov[0], ov[1], ov[2]}};
 }
 
 // 6×6 Cholesky of a spatial inertia (packed lower triangle L[21], reciprocal
@@ -323,14 +557,7 @@ __device__ __forceinline__ void load_xf(const LaneCtx<R>& c, int b, int planar, 
   const int base = sizeof(R) == 8 ? c.L.I + 12 * b : c.L.RF + 12 * b;
   auto at = [&](int e) -> R { return sizeof(R) == 8 ? R(c.d(base + e)) : c.r(base + e); };
   if (planar >= 0) {
-    const int i1 = (planar + 1) % 3, i2 = (planar + 2) % 3;
-    const R co = at(0), si = at(1);
-#pragma unroll
-    for (int e = 0; e < 9; ++e) Rr.a[e] = (e % 4 == 0) ? R(1) : R(0);
-    Rr.a[3 * i1 + i1] = co;
-    Rr.a[3 * i1 + i2] = -si;
-    Rr.a[3 * i2 + i1] = si;
-    Rr.a[3 * i2 + i2] = co;
+    Rr = planar_rot<R>(planar, at(0), at(1));
   } else {
 #pragma unroll
     for (int k = 0; k < 9; ++k) Rr.a[k] = at(k);
@@ -362,6 +589,179 @@ __device__ __forceinline__ void store_svd(const LaneCtx<R>& c, int base, const S
   c.d(base + 3) = s.v.x;
   c.d(base + 4) = s.v.y;
   c.d(base + 5) = s.v.z;
+}
+
+// Pass 2 of the mixed form: articulated inertias, U, D and the congruence to
+// the parent in double-float, from the FP32 model and the FP32 transforms of
+// pass 1; bias forces in FP32 (FP64 for contact mechanisms, as in the FP64
+// form).  A 1-DOF joint's DU record holds FF words (U, 1/D, u); a floating
+// joint's holds the FP64 record of the FP64 form.
+template <typename R>
+__device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q, Col<double> tau, bool have_tau,
+                                             bool contacts) {
+  using V = V3<R>;
+  using VD = V3<double>;
+  int st = 0;
+  ABIF carryI;
+  SV<R> carryP;
+  int ctarget = -1;
+  for (int b = c.nb - 1; b >= 0; --b) {
+    const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
+    const uint32_t fl = w1 & 255;
+    const int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
+    const int tb = TOPO_D * b;
+    ABIF IA = body_abi_ff(c, tb);
+    SV<double> pAd;
+    SV<R> pA;
+    if (contacts) {
+      pAd = load_svd(c, c.L.F + 6 * b);
+      if (ctarget == b) pAd = pAd + sv_d(carryP);
+      pA = sv_r<R>(pAd);
+    } else {
+      pA = load_sv(c, c.L.F + 6 * b);
+      if (ctarget == b) pA = pA + carryP;
+    }
+    if (fl & BF_BRANCH) abi_add(IA, load_abi_ff(c, c.L.AI + ABI_D * b));
+    if (ctarget == b) abi_add(IA, carryI);
+    const SV<R> cb = load_sv(c, c.L.A + 6 * b);
+    SV<R> pa;
+    const bool to_parent = parent != 0;
+    const int planar = planar_axis(type, fl);
+    if (type == 1 || type == 2) {
+      FF Uw[3], Uv[3], D;
+      const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
+      if (type == 1 && (fl & BF_AXIS_PRINCIPAL)) {  // a = ±e_k: U = ±(A[:,k], row k of B), D = A_kk
+        const int k = (int)bf_axis_index(fl);
+        Uw[0] = pick3(k, IA.A[0], IA.A[3], IA.A[4]);
+        Uw[1] = pick3(k, IA.A[3], IA.A[1], IA.A[5]);
+        Uw[2] = pick3(k, IA.A[4], IA.A[5], IA.A[2]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Uv[i] = pick3(k, IA.B[i], IA.B[3 + i], IA.B[6 + i]);
+        if (fl & BF_AXIS_NEG) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            Uw[i] = ff_neg(Uw[i]);
+            Uv[i] = ff_neg(Uv[i]);
+          }
+        }
+        D = pick3(k, IA.A[0], IA.A[1], IA.A[2]);
+      } else if (type == 1) {  // U = I (a, 0) = (A a, Bᵀ a)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          Uw[i] = ff_dot3f(symget(IA.A, i, 0), symget(IA.A, i, 1), symget(IA.A, i, 2), ax.x, ax.y, ax.z);
+          Uv[i] = ff_dot3f(IA.B[i], IA.B[3 + i], IA.B[6 + i], ax.x, ax.y, ax.z);
+        }
+        D = ff_dot3f(Uw[0], Uw[1], Uw[2], ax.x, ax.y, ax.z);
+      } else {  // U = I (0, a) = (B a, C a)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          Uw[i] = ff_dot3f(IA.B[3 * i], IA.B[3 * i + 1], IA.B[3 * i + 2], ax.x, ax.y, ax.z);
+          Uv[i] = ff_dot3f(symget(IA.C, i, 0), symget(IA.C, i, 1), symget(IA.C, i, 2), ax.x, ax.y, ax.z);
+        }
+        D = ff_dot3f(Uv[0], Uv[1], Uv[2], ax.x, ax.y, ax.z);
+      }
+      // u = τ + τ_spring − Sᵀ p^A (FP64, as in the FP64 form, then split)
+      double u = have_tau ? tau[vo] : 0.0;
+      if (type == 2 && (w1 & BF_SPRING) && c.springs)
+        u += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
+      if (contacts) {
+        const VD axd{c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
+        u -= type == 1 ? dot(axd, pAd.w) : dot(axd, pAd.v);
+      } else {
+        u -= double(type == 1 ? dot(ax, pA.w) : dot(ax, pA.v));
+      }
+      if (type == 1) {  // revolute armature (src/hybrid/articulated/mod.rs:244-247)
+        const float arm = c.t(tb + TD_ARMATURE);
+        if (arm != 0.0f) D = ff_add(D, ff(arm));
+      }
+      if (!(D.hi > 0.0f)) st |= 2;  // GPB_ST_CHOL_FAIL
+      const FF Dinv = ff_rcp(D);
+      const FF uf = ff_from_double(u);
+      const int du = c.L.DU + DU_D * vo;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        ffw(c, du + i) = Uw[i];
+        ffw(c, du + 3 + i) = Uv[i];
+      }
+      ffw(c, du + 6) = Dinv;
+      ffw(c, du + 7) = uf;
+      if (to_parent) {
+        // I^a = I^A − U D⁻¹ Uᵀ ; p^a = p^A + I^a c + U D⁻¹ u (FP32)
+        FF Ww[3], Wv[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          Ww[i] = ff_mul(Uw[i], Dinv);
+          Wv[i] = ff_mul(Uv[i], Dinv);
+        }
+        const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          IA.A[k] = ff_fms(IA.A[k], Ww[ii[k]], Uw[jj[k]]);
+          IA.C[k] = ff_fms(IA.C[k], Wv[ii[k]], Uv[jj[k]]);
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) IA.B[3 * i + j] = ff_fms(IA.B[3 * i + j], Ww[i], Uv[j]);
+        const R ud = ff_mul(uf, Dinv).hi;
+        const SV<R> Ur{{Uw[0].hi, Uw[1].hi, Uw[2].hi}, {Uv[0].hi, Uv[1].hi, Uv[2].hi}};
+        pa = pA + abi_mul_hi(IA, cb) + scale(Ur, ud);
+      }
+    } else if (type == 3) {  // floating joint: the FP64 6×6 solve of the FP64 form
+      double L[21], dinv[6];
+      if (!chol6(abi_to_double(IA), L, dinv)) st |= 2;
+      const int du = c.L.DU + DU_D * vo;
+#pragma unroll
+      for (int k = 0; k < 21; ++k) c.d(du + k) = L[k];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) c.d(du + 21 + k) = dinv[k];
+      const SV<double> pp = contacts ? pAd : sv_d(pA);
+      const double pv6[6] = {pp.w.x, pp.w.y, pp.w.z, pp.v.x, pp.v.y, pp.v.z};
+      R pa6[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const double u = (have_tau ? tau[vo + k] : 0.0) - pv6[k];
+        c.d(du + 27 + k) = u;
+        pa6[k] = R(double(pv6[k]) + u);  // floating joint: I^a = 0, p^a = p^A + u
+      }
+      pa = {{pa6[0], pa6[1], pa6[2]}, {pa6[3], pa6[4], pa6[5]}};
+    } else {  // fixed joint: I^a = I^A, p^a = p^A + I^A c
+      pa = pA + abi_mul_hi(IA, cb);
+    }
+    if (to_parent) {
+      const int pb = parent - 1;
+      M3<R> RrR;
+      V tr;
+      load_xf(c, b, planar, RrR, tr);
+      if (type != 3) {
+        const R co = planar >= 0 ? c.r(c.L.RF + 12 * b) : R(1);
+        const R si = planar >= 0 ? c.r(c.L.RF + 12 * b + 1) : R(0);
+        const ABIF Ip = abi_to_parent(IA, RrR, tr, planar, co, si);
+        if (pb == b - 1) {
+          carryI = Ip;
+        } else {
+          ABIF acc = load_abi_ff(c, c.L.AI + ABI_D * pb);
+          abi_add(acc, Ip);
+          store_abi_ff(c, c.L.AI + ABI_D * pb, acc);
+        }
+      } else if (pb == b - 1) {
+        carryI = ABIF{};  // floating joint below the parent: I^a = 0
+      }
+      // force to the parent frame: (Rr n + t × Rr f, Rr f)
+      const SV<R> fp = force_to_parent(RrR, tr, pa);
+      if (pb == b - 1) {
+        carryP = fp;
+        ctarget = pb;
+      } else {
+        if (contacts) store_svd(c, c.L.F + 6 * pb, load_svd(c, c.L.F + 6 * pb) + sv_d(fp));
+        else store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
+        ctarget = -1;
+      }
+    } else {
+      ctarget = -1;
+    }
+  }
+  return st;
 }
 
 // One dynamics evaluation by the articulated-body algorithm.  q̈ into qdd;
@@ -409,8 +809,10 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     M3<double> Rd = eye3<double>();
     VD td{c.td(tb + TD_TINIT), c.td(tb + TD_TINIT + 1), c.td(tb + TD_TINIT + 2)};
     M3<R> Rr;
+    double pco = 1.0, psi = 0.0;  // (cos, sin) of a planar joint, FP64 and in R
+    R rco = R(1), rsi = R(0);
     if (planar) {  // rotation about ±e_k: only the (k+1, k+2) plane turns
-      const int k = (int)bf_axis_index(fl), i1 = (k + 1) % 3, i2 = (k + 2) % 3;
+      const int k = (int)bf_axis_index(fl);
       double co, si;
       R cor, sir;
       if (wide) {
@@ -429,16 +831,12 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         si = -si;
         sir = -sir;
       }
-      Rd.a[3 * i1 + i1] = co;
-      Rd.a[3 * i1 + i2] = -si;
-      Rd.a[3 * i2 + i1] = si;
-      Rd.a[3 * i2 + i2] = co;
-#pragma unroll
-      for (int e = 0; e < 9; ++e) Rr.a[e] = (e % 4 == 0) ? R(1) : R(0);
-      Rr.a[3 * i1 + i1] = cor;
-      Rr.a[3 * i1 + i2] = -sir;
-      Rr.a[3 * i2 + i1] = sir;
-      Rr.a[3 * i2 + i2] = cor;
+      Rd = planar_rot<double>(k, co, si);
+      Rr = planar_rot<R>(k, cor, sir);
+      pco = co;
+      psi = si;
+      rco = cor;
+      rsi = sir;
     } else {
       M3<double> Rid = eye3<double>();
       if (!rid) {
@@ -582,25 +980,26 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         store_cuboid(c, uslot - 1, b, Rw, posw, omw, mul(Rw, vld) - cross(omw, posw));
       }
     }
-    // records for the inward and second outward passes: (Rrel, t); a planar
-    // rotation keeps only its (cos, sin) — the other entries are 0 and 1 — so
-    // the passes that read it back touch 5 rows instead of 12
-    if (planar) {
-      const int k = (int)bf_axis_index(fl), i1 = (k + 1) % 3, i2 = (k + 2) % 3;
-      c.d(c.L.I + 12 * b) = Rd.a[3 * i1 + i1];
-      c.d(c.L.I + 12 * b + 1) = Rd.a[3 * i2 + i1];
-    } else {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) c.d(c.L.I + 12 * b + k) = Rd.a[k];
-    }
-    c.d(c.L.I + 12 * b + 9) = td.x;
-    c.d(c.L.I + 12 * b + 10) = td.y;
-    c.d(c.L.I + 12 * b + 11) = td.z;
-    if (sizeof(R) == 4) {
+    // records for the inward and second outward passes: (Rrel, t) in R (the
+    // FP64 form's FP64 record; the mixed form's FP32 record, which its
+    // double-float inward pass reads too); a planar rotation keeps only its
+    // (cos, sin) — the other entries are 0 and 1 — so the passes that read it
+    // back touch 5 rows instead of 12
+    if (sizeof(R) == 8) {
       if (planar) {
-        const int k = (int)bf_axis_index(fl), i1 = (k + 1) % 3, i2 = (k + 2) % 3;
-        c.r(c.L.RF + 12 * b) = Rr.a[3 * i1 + i1];
-        c.r(c.L.RF + 12 * b + 1) = Rr.a[3 * i2 + i1];
+        c.d(c.L.I + 12 * b) = pco;
+        c.d(c.L.I + 12 * b + 1) = psi;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) c.d(c.L.I + 12 * b + k) = Rd.a[k];
+      }
+      c.d(c.L.I + 12 * b + 9) = td.x;
+      c.d(c.L.I + 12 * b + 10) = td.y;
+      c.d(c.L.I + 12 * b + 11) = td.z;
+    } else {
+      if (planar) {
+        c.r(c.L.RF + 12 * b) = rco;
+        c.r(c.L.RF + 12 * b + 1) = rsi;
       } else {
 #pragma unroll
         for (int k = 0; k < 9; ++k) c.r(c.L.RF + 12 * b + k) = Rr.a[k];
@@ -613,7 +1012,9 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     if (contacts) store_svd(c, c.L.F + 6 * b, sv_d(p) + wc);  // bias forces of contact mechanisms: FP64
     else store_sv(c, c.L.F + 6 * b, p);
     if (fl & BF_BRANCH) {
-      store_abi(c, c.L.AI + ABI_D * b, ABI{});  // accumulator for children other than b+1
+      // accumulator for children other than b+1
+      if (sizeof(R) == 8) store_abi(c, c.L.AI + ABI_D * b, ABI{});
+      else store_abi_ff(c, c.L.AI + ABI_D * b, ABIF{});
       store_sv(c, c.L.V + 6 * b, vb);
       if (contacts) {
 #pragma unroll
@@ -639,166 +1040,176 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
   // ---- pass 2 (inward): articulated inertias and bias forces --------------
   // A child that is the next body (every link of a chain) hands its terms to
   // the parent in registers; other children accumulate into the parent's slot.
-  ABI carryI;
-  SV<R> carryP;
-  int ctarget = -1;
-  for (int b = c.nb - 1; b >= 0; --b) {
-    const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
-    const uint32_t fl = w1 & 255;
-    const int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
-    const int tb = TOPO_D * b;
-    ABI IA = body_abi(c, tb);
-    SV<double> pAd;  // FP64 copy (contact mechanisms) for u
-    SV<R> pA;
-    if (contacts) {
-      pAd = load_svd(c, c.L.F + 6 * b);
-      if (ctarget == b) pAd = pAd + sv_d(carryP);
-      pA = sv_r<R>(pAd);
-    } else {
-      pA = load_sv(c, c.L.F + 6 * b);
-      if (ctarget == b) pA = pA + carryP;
-    }
-    if (fl & BF_BRANCH) abi_add(IA, load_abi(c, c.L.AI + ABI_D * b));
-    if (ctarget == b) abi_add(IA, carryI);
-    const SV<R> cb = load_sv(c, c.L.A + 6 * b);
-    SV<R> pa;  // bias force handed to the parent
-    const bool to_parent = parent != 0;
-    if (type == 1 || type == 2) {
-      double Uw[3], Uv[3], D;
-      if (type == 1 && (fl & BF_AXIS_PRINCIPAL)) {  // a = ±e_k: U = ±(A[:,k], row k of B), D = A_kk
-        const int k = (int)bf_axis_index(fl);
-        const double sg = (fl & BF_AXIS_NEG) ? -1.0 : 1.0;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          Uw[i] = sg * symget(IA.A, i, k);
-          Uv[i] = sg * IA.B[3 * k + i];
-        }
-        D = IA.A[k];
-      } else {
-        const double ax[3] = {c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
-        if (type == 1) {  // U = I (a, 0) = (A a, Bᵀ a)
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            Uw[i] = symget(IA.A, i, 0) * ax[0] + symget(IA.A, i, 1) * ax[1] + symget(IA.A, i, 2) * ax[2];
-            Uv[i] = IA.B[i] * ax[0] + IA.B[3 + i] * ax[1] + IA.B[6 + i] * ax[2];
-          }
-          D = ax[0] * Uw[0] + ax[1] * Uw[1] + ax[2] * Uw[2];
-        } else {  // U = I (0, a) = (B a, C a)
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            Uw[i] = IA.B[3 * i] * ax[0] + IA.B[3 * i + 1] * ax[1] + IA.B[3 * i + 2] * ax[2];
-            Uv[i] = symget(IA.C, i, 0) * ax[0] + symget(IA.C, i, 1) * ax[1] + symget(IA.C, i, 2) * ax[2];
-          }
-          D = ax[0] * Uv[0] + ax[1] * Uv[1] + ax[2] * Uv[2];
-        }
-      }
-      // u = τ + τ_spring − Sᵀ p^A
-      const V axr{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
-      double u = have_tau ? tau[vo] : 0.0;
-      if (type == 2 && (w1 & BF_SPRING) && c.springs)
-        u += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
+  if constexpr (sizeof(R) == 4) {
+    st |= aba_inward_ff(c, q, tau, have_tau, contacts);
+  } else {
+    ABI carryI;
+    SV<R> carryP;
+    int ctarget = -1;
+    for (int b = c.nb - 1; b >= 0; --b) {
+      const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
+      const uint32_t fl = w1 & 255;
+      const int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
+      const int tb = TOPO_D * b;
+      ABI IA = body_abi(c, tb);
+      SV<double> pAd;  // FP64 copy (contact mechanisms) for u
+      SV<R> pA;
       if (contacts) {
-        const VD axd{c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
-        u -= type == 1 ? dot(axd, pAd.w) : dot(axd, pAd.v);
+        pAd = load_svd(c, c.L.F + 6 * b);
+        if (ctarget == b) pAd = pAd + sv_d(carryP);
+        pA = sv_r<R>(pAd);
       } else {
-        u -= double(type == 1 ? dot(axr, pA.w) : dot(axr, pA.v));
+        pA = load_sv(c, c.L.F + 6 * b);
+        if (ctarget == b) pA = pA + carryP;
       }
-      if (type == 1) D += c.td(tb + TD_ARMATURE);  // revolute armature (src/hybrid/articulated/mod.rs:244-247)
-      if (!(D > 0.0)) st |= 2;  // GPB_ST_CHOL_FAIL
-      const double Dinv = 1.0 / D;
-      const int du = c.L.DU + DU_D * vo;
+      if (fl & BF_BRANCH) abi_add(IA, load_abi(c, c.L.AI + ABI_D * b));
+      if (ctarget == b) abi_add(IA, carryI);
+      const SV<R> cb = load_sv(c, c.L.A + 6 * b);
+      SV<R> pa;  // bias force handed to the parent
+      const bool to_parent = parent != 0;
+      if (type == 1 || type == 2) {
+        double Uw[3], Uv[3], D;
+        if (type == 1 && (fl & BF_AXIS_PRINCIPAL)) {  // a = ±e_k: U = ±(A[:,k], row k of B), D = A_kk
+          const int k = (int)bf_axis_index(fl);
+          Uw[0] = pick3(k, IA.A[0], IA.A[3], IA.A[4]);
+          Uw[1] = pick3(k, IA.A[3], IA.A[1], IA.A[5]);
+          Uw[2] = pick3(k, IA.A[4], IA.A[5], IA.A[2]);
 #pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        c.d(du + i) = Uw[i];
-        c.d(du + 3 + i) = Uv[i];
-      }
-      c.d(du + 6) = Dinv;
-      c.d(du + 7) = u;
-      if (to_parent) {
-        // I^a = I^A − U D⁻¹ Uᵀ (FP64) ; p^a = p^A + I^a c + U D⁻¹ u (R)
-        double Ww[3], Wv[3];
+          for (int i = 0; i < 3; ++i) Uv[i] = pick3(k, IA.B[i], IA.B[3 + i], IA.B[6 + i]);
+          if (fl & BF_AXIS_NEG) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              Uw[i] = -Uw[i];
+              Uv[i] = -Uv[i];
+            }
+          }
+          D = pick3(k, IA.A[0], IA.A[1], IA.A[2]);
+        } else {
+          const double ax[3] = {c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
+          if (type == 1) {  // U = I (a, 0) = (A a, Bᵀ a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              Uw[i] = symget(IA.A, i, 0) * ax[0] + symget(IA.A, i, 1) * ax[1] + symget(IA.A, i, 2) * ax[2];
+              Uv[i] = IA.B[i] * ax[0] + IA.B[3 + i] * ax[1] + IA.B[6 + i] * ax[2];
+            }
+            D = ax[0] * Uw[0] + ax[1] * Uw[1] + ax[2] * Uw[2];
+          } else {  // U = I (0, a) = (B a, C a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              Uw[i] = IA.B[3 * i] * ax[0] + IA.B[3 * i + 1] * ax[1] + IA.B[3 * i + 2] * ax[2];
+              Uv[i] = symget(IA.C, i, 0) * ax[0] + symget(IA.C, i, 1) * ax[1] + symget(IA.C, i, 2) * ax[2];
+            }
+            D = ax[0] * Uv[0] + ax[1] * Uv[1] + ax[2] * Uv[2];
+          }
+        }
+        // u = τ + τ_spring − Sᵀ p^A
+        const V axr{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
+        double u = have_tau ? tau[vo] : 0.0;
+        if (type == 2 && (w1 & BF_SPRING) && c.springs)
+          u += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
+        if (contacts) {
+          const VD axd{c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
+          u -= type == 1 ? dot(axd, pAd.w) : dot(axd, pAd.v);
+        } else {
+          u -= double(type == 1 ? dot(axr, pA.w) : dot(axr, pA.v));
+        }
+        if (type == 1) D += c.td(tb + TD_ARMATURE);  // revolute armature (src/hybrid/articulated/mod.rs:244-247)
+        if (!(D > 0.0)) st |= 2;  // GPB_ST_CHOL_FAIL
+        const double Dinv = 1.0 / D;
+        const int du = c.L.DU + DU_D * vo;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          Ww[i] = Uw[i] * Dinv;
-          Wv[i] = Uv[i] * Dinv;
+          c.d(du + i) = Uw[i];
+          c.d(du + 3 + i) = Uv[i];
         }
-        const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+        c.d(du + 6) = Dinv;
+        c.d(du + 7) = u;
+        if (to_parent) {
+          // I^a = I^A − U D⁻¹ Uᵀ (FP64) ; p^a = p^A + I^a c + U D⁻¹ u (R)
+          double Ww[3], Wv[3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            Ww[i] = Uw[i] * Dinv;
+            Wv[i] = Uv[i] * Dinv;
+          }
+          const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            IA.A[k] -= Ww[ii[k]] * Uw[jj[k]];
+            IA.C[k] -= Wv[ii[k]] * Uv[jj[k]];
+          }
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) IA.B[3 * i + j] -= Ww[i] * Uv[j];
+          const R ud = R(u * Dinv);
+          const SV<R> Ur{{R(Uw[0]), R(Uw[1]), R(Uw[2])}, {R(Uv[0]), R(Uv[1]), R(Uv[2])}};
+          pa = pA + abi_mul_r<R>(IA, cb) + scale(Ur, ud);
+        }
+      } else if (type == 3) {
+        double L[21], dinv[6];
+        if (!chol6(IA, L, dinv)) st |= 2;
+        const int du = c.L.DU + DU_D * vo;
+#pragma unroll
+        for (int k = 0; k < 21; ++k) c.d(du + k) = L[k];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) c.d(du + 21 + k) = dinv[k];
+        const SV<double> pp = contacts ? pAd : sv_d(pA);
+        const double pv6[6] = {pp.w.x, pp.w.y, pp.w.z, pp.v.x, pp.v.y, pp.v.z};
+        R pa6[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-          IA.A[k] -= Ww[ii[k]] * Uw[jj[k]];
-          IA.C[k] -= Wv[ii[k]] * Uv[jj[k]];
+          const double u = (have_tau ? tau[vo + k] : 0.0) - pv6[k];
+          c.d(du + 27 + k) = u;
+          pa6[k] = R(double(pv6[k]) + u);  // floating joint: I^a = 0, p^a = p^A + u
         }
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-          for (int j = 0; j < 3; ++j) IA.B[3 * i + j] -= Ww[i] * Uv[j];
-        const R ud = R(u * Dinv);
-        const SV<R> Ur{{R(Uw[0]), R(Uw[1]), R(Uw[2])}, {R(Uv[0]), R(Uv[1]), R(Uv[2])}};
-        pa = pA + abi_mul_r<R>(IA, cb) + scale(Ur, ud);
+        pa = {{pa6[0], pa6[1], pa6[2]}, {pa6[3], pa6[4], pa6[5]}};
+      } else {  // fixed joint: I^a = I^A, p^a = p^A + I^A c
+        pa = pA + abi_mul_r<R>(IA, cb);
       }
-    } else if (type == 3) {
-      double L[21], dinv[6];
-      if (!chol6(IA, L, dinv)) st |= 2;
-      const int du = c.L.DU + DU_D * vo;
+      if (to_parent) {
+        const int pb = parent - 1;
+        if (type != 3) {
+          double Rr[9];
+          const VD t{c.d(c.L.I + 12 * b + 9), c.d(c.L.I + 12 * b + 10), c.d(c.L.I + 12 * b + 11)};
+          const int planar = planar_axis(type, fl);
+          double co = 1.0, si = 0.0;
+          if (planar >= 0) {  // (cos, sin) record; abi_to_parent does not read Rr then
+            co = c.d(c.L.I + 12 * b);
+            si = c.d(c.L.I + 12 * b + 1);
 #pragma unroll
-      for (int k = 0; k < 21; ++k) c.d(du + k) = L[k];
+            for (int k = 0; k < 9; ++k) Rr[k] = 0.0;
+          } else {
 #pragma unroll
-      for (int k = 0; k < 6; ++k) c.d(du + 21 + k) = dinv[k];
-      const SV<double> pp = contacts ? pAd : sv_d(pA);
-      const double pv6[6] = {pp.w.x, pp.w.y, pp.w.z, pp.v.x, pp.v.y, pp.v.z};
-      R pa6[6];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        const double u = (have_tau ? tau[vo + k] : 0.0) - pv6[k];
-        c.d(du + 27 + k) = u;
-        pa6[k] = R(double(pv6[k]) + u);  // floating joint: I^a = 0, p^a = p^A + u
-      }
-      pa = {{pa6[0], pa6[1], pa6[2]}, {pa6[3], pa6[4], pa6[5]}};
-    } else {  // fixed joint: I^a = I^A, p^a = p^A + I^A c
-      pa = pA + abi_mul_r<R>(IA, cb);
-    }
-    if (to_parent) {
-      const int pb = parent - 1;
-      if (type != 3) {
-        double Rr[9];
-        const VD t{c.d(c.L.I + 12 * b + 9), c.d(c.L.I + 12 * b + 10), c.d(c.L.I + 12 * b + 11)};
-        const int planar = planar_axis(type, fl);
-        double co = 1.0, si = 0.0;
-        if (planar >= 0) {  // (cos, sin) record; abi_to_parent does not read Rr then
-          co = c.d(c.L.I + 12 * b);
-          si = c.d(c.L.I + 12 * b + 1);
-#pragma unroll
-          for (int k = 0; k < 9; ++k) Rr[k] = 0.0;
-        } else {
-#pragma unroll
-          for (int k = 0; k < 9; ++k) Rr[k] = c.d(c.L.I + 12 * b + k);
+            for (int k = 0; k < 9; ++k) Rr[k] = c.d(c.L.I + 12 * b + k);
+          }
+          const ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si);
+          if (pb == b - 1) {
+            carryI = Ip;
+          } else {
+            ABI acc = load_abi(c, c.L.AI + ABI_D * pb);
+            abi_add(acc, Ip);
+            store_abi(c, c.L.AI + ABI_D * pb, acc);
+          }
+        } else if (pb == b - 1) {
+          carryI = ABI{};  // floating joint below the parent: I^a = 0
         }
-        const ABI Ip = abi_to_parent(IA, Rr, t, planar, co, si);
+        // force to the parent frame: (Rr n + t × Rr f, Rr f)
+        M3<R> RrR;
+        V tr;
+        load_xf(c, b, planar_axis(type, fl), RrR, tr);
+        const SV<R> fp = force_to_parent(RrR, tr, pa);
         if (pb == b - 1) {
-          carryI = Ip;
+          carryP = fp;
+          ctarget = pb;
         } else {
-          ABI acc = load_abi(c, c.L.AI + ABI_D * pb);
-          abi_add(acc, Ip);
-          store_abi(c, c.L.AI + ABI_D * pb, acc);
+          if (contacts) store_svd(c, c.L.F + 6 * pb, load_svd(c, c.L.F + 6 * pb) + sv_d(fp));
+          else store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
+          ctarget = -1;
         }
-      } else if (pb == b - 1) {
-        carryI = ABI{};  // floating joint below the parent: I^a = 0
-      }
-      // force to the parent frame: (Rr n + t × Rr f, Rr f)
-      M3<R> RrR;
-      V tr;
-      load_xf(c, b, planar_axis(type, fl), RrR, tr);
-      const SV<R> fp = force_to_parent(RrR, tr, pa);
-      if (pb == b - 1) {
-        carryP = fp;
-        ctarget = pb;
       } else {
-        if (contacts) store_svd(c, c.L.F + 6 * pb, load_svd(c, c.L.F + 6 * pb) + sv_d(fp));
-        else store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
         ctarget = -1;
       }
-    } else {
-      ctarget = -1;
     }
   }
   // ---- pass 3 (outward): accelerations -------------------------------------
@@ -824,17 +1235,31 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     a = a + load_sv(c, c.L.A + 6 * b);
     const int du = c.L.DU + DU_D * vo;
     if (type == 1 || type == 2) {
-      const double aw[3] = {double(a.w.x), double(a.w.y), double(a.w.z)};
-      const double av[3] = {double(a.v.x), double(a.v.y), double(a.v.z)};
-      double ua = 0.0;
+      double x;
+      R xr;
+      if constexpr (sizeof(R) == 4) {  // x = D⁻¹ (u − Uᵀ a') in double-float
+        FF ua = ff_lin2(ffw(c, du), a.w.x, ffw(c, du + 1), a.w.y);
+        ua = ff_fmaf(ffw(c, du + 2), a.w.z, ua);
+        ua = ff_fmaf(ffw(c, du + 3), a.v.x, ua);
+        ua = ff_fmaf(ffw(c, du + 4), a.v.y, ua);
+        ua = ff_fmaf(ffw(c, du + 5), a.v.z, ua);
+        const FF xf = ff_mul(ffw(c, du + 6), ff_sub(ffw(c, du + 7), ua));
+        x = ff_to_double(xf);
+        xr = xf.hi;
+      } else {
+        const double aw[3] = {double(a.w.x), double(a.w.y), double(a.w.z)};
+        const double av[3] = {double(a.v.x), double(a.v.y), double(a.v.z)};
+        double ua = 0.0;
 #pragma unroll
-      for (int i = 0; i < 3; ++i) ua += c.d(du + i) * aw[i] + c.d(du + 3 + i) * av[i];
-      const double x = c.d(du + 6) * (c.d(du + 7) - ua);
+        for (int i = 0; i < 3; ++i) ua += c.d(du + i) * aw[i] + c.d(du + 3 + i) * av[i];
+        x = c.d(du + 6) * (c.d(du + 7) - ua);
+        xr = R(x);
+      }
       qdd[vo] = x;
       if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
       const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
-      if (type == 1) a.w = a.w + ax * R(x);
-      else a.v = a.v + ax * R(x);
+      if (type == 1) a.w = a.w + ax * xr;
+      else a.v = a.v + ax * xr;
     } else if (type == 3) {
       // q̈ = D⁻¹ (u − Uᵀ a') with U = D = I^A, i.e. D⁻¹ u − a'; then a = D⁻¹ u
       double x[6];

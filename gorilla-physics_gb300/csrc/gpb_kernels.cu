@@ -23,6 +23,7 @@
 #include "gpb.h"
 
 #include "gpb_device.cuh"
+#include "gpb_ff.cuh"
 #include "gpb_internal.h"
 #include "gpb_rng.h"
 #include "gpb_collide.cuh"
