@@ -609,8 +609,12 @@ extern "C" int gpb_batch_autotune(gpb_batch* b, double dt, int integrator, int p
   };
   CUDA_TRY(save_restore(true));
   const int keep_w = b->warps_per_sm, keep_c = b->coop_min_dof;
+  // 4 warps per SM and every further multiple of 4 the kernel's registers
+  // leave room for, up to 16
+  int wmax = 8;
+  CUDA_TRY(simulate_max_warps_per_sm(precision, &wmax));
   std::vector<std::pair<int, int>> cand;
-  for (int w : {4, 8}) {
+  for (int w = 4; w <= 16 && (w == 4 || w <= wmax); w += 4) {
     cand.push_back({w, 0});
     if (precision != GPB_MIXED_REFINED && b->algorithm == GPB_ALGO_CRBA && b->npacks > 0 &&
         b->packs_h[0].minnv >= 32)

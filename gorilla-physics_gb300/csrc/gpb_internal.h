@@ -231,6 +231,8 @@ struct StepParams {
 cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes_per_instance,
                             int num_sms, int warps_per_sm, cudaStream_t s);
 cudaError_t launch_dynamics(const DeviceBatch& b, const StepParams& p, cudaStream_t s);
+// Resident warps per SM the step kernel of `precision` can hold (registers).
+cudaError_t simulate_max_warps_per_sm(int precision, int* warps);
 cudaError_t launch_scatter(const int64_t* map, int64_t slots, const double* src, double* dst,
                            cudaStream_t s);
 cudaError_t launch_gather(const int64_t* map, int64_t slots, const double* src, double* dst,

@@ -1356,6 +1356,14 @@ cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes
   return cudaGetLastError();
 }
 
+cudaError_t simulate_max_warps_per_sm(int precision, int* warps) {
+  auto kern = precision == 2 ? simulate_kernel<2> : (precision == 1 ? simulate_kernel<1> : simulate_kernel<0>);
+  int per_sm = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0);
+  *warps = 4 * per_sm;
+  return e;
+}
+
 cudaError_t launch_dynamics(const DeviceBatch& b, const StepParams& p, cudaStream_t s) {
   const int threads = 128;
   unsigned grid = (unsigned)((b.npacks + 3) / 4);

@@ -364,8 +364,9 @@ int gpb_free_velocity(gpb_batch* batch, double dt, const double* tau, int precis
 
 /* Autotuner: times `trial_steps` steps of this batch (its own mechanisms,
  * state, step size, integrator, precision and control law) for each launch
- * shape (4 or 8 resident warps per SM; block-cooperative packs off or from 32 /
- * 40 DOF when the batch has such packs), keeps the fastest with
+ * shape (4, 8, 12 or 16 resident warps per SM, as many as the step kernel's
+ * registers allow; block-cooperative packs off or from 32 / 40 DOF when the
+ * batch has such packs), keeps the fastest with
  * gpb_batch_set_launch / gpb_batch_set_coop and reports it.  The batch's q, v,
  * torques and status words are restored afterwards; results of later calls do
  * not depend on the choice (every shape computes the same bits). */
