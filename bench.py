@@ -398,6 +398,11 @@ def run_gpu(args):
             "fp64": "articulated-body algorithm flops (gpb.flops.aba_model_flops)",
             "mixed": "FP64 share of the mixed articulated-body algorithm (gpb.flops.aba_model_flops(mixed=True))",
             "refined": "CRBA-equivalent flops (the FP64 residual is a part of them)"}
+    # The mixed form runs its precision-critical recursion in double-float on the
+    # FP32 pipes: no single pipe is near its peak, and its roofline is the SM's
+    # instruction issue rate (the warp-instruction rate of the measured FP32 FMA
+    # microbenchmark) against its executed warp instructions per instance-step.
+    warp_inst_peak = p32 * 1e12 / 64 / 1e9  # G warp-instructions/s (64 flops per FFMA warp instruction)
 
     # DRAM bytes per instance-step from the committed ncu capture (small case of the
     # same workload), scaled to this launch's completed instance-steps
@@ -415,10 +420,19 @@ def run_gpu(args):
     def roof(name, res):
         ach = res["flops"] / (res["kernel_ms"] * 1e-3) / 1e12
         per = res["flops"] / max(res["done"], 1.0)
-        out = {"bound": "fp64", "achieved": ach, "peak": p64, "unit": "TFLOP/s", "frac": ach / p64,
-               "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (gpb_fma_peak), this run",
-               "work": f"{per:.0f} FP64 flops per completed instance-step (mean): {WORK[name]}"}
         t = traffic_per.get(name)
+        if name == "mixed" and t and "warp_instructions_per_instance_step" in t and not args.mix_chains:
+            wi = t["warp_instructions_per_instance_step"]
+            ach_i = wi * res["done"] / (res["kernel_ms"] * 1e-3) / 1e9
+            out = {"bound": "issue", "achieved": ach_i, "peak": warp_inst_peak, "unit": "G warp-instructions/s",
+                   "frac": ach_i / warp_inst_peak, "traffic": None,
+                   "peak_source": "measured FP32 FMA microbenchmark (gpb_fma_peak), this run, in warp instructions",
+                   "work": f"{wi:.0f} executed warp instructions per instance-step (ncu, {t['capture']}); "
+                           f"{per:.0f} FP64 flops per instance-step remain on the FP64 pipe"}
+        else:
+            out = {"bound": "fp64", "achieved": ach, "peak": p64, "unit": "TFLOP/s", "frac": ach / p64,
+                   "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (gpb_fma_peak), this run",
+                   "work": f"{per:.0f} FP64 flops per completed instance-step (mean): {WORK[name]}"}
         if t and not args.mix_chains:
             bytes_launch = t["dram_bytes_per_instance_step"] * res["done"]
             out["traffic"] = bytes_launch
@@ -430,7 +444,7 @@ def run_gpu(args):
         return out
 
     DTYPE = {"fp64_crba": "f64", "fp64": "f64",
-             "mixed": "f32 kinematics/bias + f64 articulated inertias + f64 state",
+             "mixed": "f32 kinematics/bias + double-f32 articulated inertias + f64 state",
              "refined": "f32 solve + f64 residual refinement + f64 state"}
     ALGO = {"fp64_crba": "CRBA + Cholesky (the reference's route)", "fp64": "articulated-body algorithm",
             "mixed": "articulated-body algorithm", "refined": "CRBA + Cholesky, iterative refinement"}

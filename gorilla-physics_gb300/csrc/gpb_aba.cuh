@@ -394,33 +394,32 @@ __device__ __forceinline__ void gen_rotate(const float* R, const FF* B, FF* out)
     for (int j = 0; j < 3; ++j)
       out[3 * i + j] = ff_dot3f(P[3 * i], P[3 * i + 1], P[3 * i + 2], R[3 * j], R[3 * j + 1], R[3 * j + 2]);
 }
-// The shift of shift_general with an FP32 translation.
+// The shift of shift_general with an FP32 translation, in the equivalent form
+// B_p = B' + T C', A_p = A' − B_p T − (B' T)ᵀ (B_p T = B'T + T C' T).
 __device__ __forceinline__ void shift_general(const FF* A, const FF* B, const FF* Cm, V3<float> t, ABIF& o) {
-  FF W[9], BT[9];  // W = T C', BT = B' T
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    W[j] = ff_lin2(Cm[3 + j], -t.z, Cm[6 + j], t.y);
-    W[3 + j] = ff_lin2(Cm[j], t.z, Cm[6 + j], -t.x);
-    W[6 + j] = ff_lin2(Cm[j], -t.y, Cm[3 + j], t.x);
-  }
+  FF BT[9];  // B' T
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     BT[3 * i] = ff_lin2(B[3 * i + 1], t.z, B[3 * i + 2], -t.y);
     BT[3 * i + 1] = ff_lin2(B[3 * i], -t.z, B[3 * i + 2], t.x);
     BT[3 * i + 2] = ff_lin2(B[3 * i], t.y, B[3 * i + 1], -t.x);
   }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    o.B[j] = ff_add(B[j], ff_lin2(Cm[3 + j], -t.z, Cm[6 + j], t.y));
+    o.B[3 + j] = ff_add(B[3 + j], ff_lin2(Cm[j], t.z, Cm[6 + j], -t.x));
+    o.B[6 + j] = ff_add(B[6 + j], ff_lin2(Cm[j], -t.y, Cm[3 + j], t.x));
+  }
   const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
     const int i = ii[k], j = jj[k];
-    const FF wt = j == 0 ? ff_lin2(W[3 * i + 1], t.z, W[3 * i + 2], -t.y)
-                         : (j == 1 ? ff_lin2(W[3 * i], -t.z, W[3 * i + 2], t.x)
-                                   : ff_lin2(W[3 * i], t.y, W[3 * i + 1], -t.x));
-    o.A[k] = ff_sub(A[3 * i + j], ff_add3(BT[3 * i + j], BT[3 * j + i], wt));
+    const FF bpt = j == 0 ? ff_lin2(o.B[3 * i + 1], t.z, o.B[3 * i + 2], -t.y)
+                          : (j == 1 ? ff_lin2(o.B[3 * i], -t.z, o.B[3 * i + 2], t.x)
+                                    : ff_lin2(o.B[3 * i], t.y, o.B[3 * i + 1], -t.x));
+    o.A[k] = ff_sub(A[3 * i + j], ff_add(bpt, BT[3 * j + i]));
     o.C[k] = Cm[3 * i + j];
   }
-#pragma unroll
-  for (int k = 0; k < 9; ++k) o.B[k] = ff_add(B[k], W[k]);
 }
 // abi_to_parent in double-float: the child's FP32 transform (Rr, t), or its
 // (co, si) about principal axis `planar`.

@@ -78,14 +78,17 @@ def model_flops(model, integrator: int = 0) -> np.ndarray:
 #   Cholesky and solve), fixed 650
 #   contact point 130, plus 60 per body of a mechanism with contacts (FP64
 #   world poses)
-# GPB_MIXED keeps in FP64 only U, D, the articulated-inertia update, the
-# congruence and accumulation, the final q̈ dot products and everything that
-# places contacts: 275 per planar revolute body, 460 other revolute, 440
-# prismatic, 240 floating root, 380 fixed; contacts as above.
+# GPB_MIXED runs the articulated-inertia recursion and the 1-DOF q̈ solve in
+# double-float on the FP32 pipes; what stays FP64 is the state update, u, the
+# reduction of q before sin/cos, the open-loop torque draw, a floating root's
+# 6×6 Cholesky and everything that places contacts: 23 per planar revolute
+# body (ncu on 65,536 serial chains: 575 FP64 flops per instance-step), 50
+# other revolute (Rodrigues), 30 prismatic, 240 floating root, 10 fixed;
+# contacts as above.
 # ---------------------------------------------------------------------------
 
 ABA_FP64 = {"rev_planar": 620, "rev": 845, "pri": 800, "float": 440, "fixed": 650}
-ABA_MIXED_FP64 = {"rev_planar": 275, "rev": 460, "pri": 440, "float": 240, "fixed": 380}
+ABA_MIXED_FP64 = {"rev_planar": 23, "rev": 50, "pri": 30, "float": 240, "fixed": 10}
 ABA_CONTACT = 130
 ABA_POSE = 60
 
