@@ -450,17 +450,25 @@ __device__ __forceinline__ ABIF abi_to_parent(const ABIF& I, const M3<float>& Rr
   shift_general(A, B, Cm, t, o);
   return o;
 }
-// I·(w, v) from the leading FP32 parts (the bias-force update needs only FP32).
+// I·(w, v) in FP32 from the rounded entries (the bias-force update needs only FP32).
 __device__ __forceinline__ SV<float> abi_mul_hi(const ABIF& I, const SV<float>& x) {
   const float w[3] = {x.w.x, x.w.y, x.w.z}, v[3] = {x.v.x, x.v.y, x.v.z};
+  float A[6], B[9], C[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    A[k] = ff_f(I.A[k]);
+    C[k] = ff_f(I.C[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) B[k] = ff_f(I.B[k]);
   float ow[3], ov[3];
   const int s[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    ow[i] = I.A[s[i][0]].hi * w[0] + I.A[s[i][1]].hi * w[1] + I.A[s[i][2]].hi * w[2] + I.B[3 * i].hi * v[0] +
-            I.B[3 * i + 1].hi * v[1] + I.B[3 * i + 2].hi * v[2];
-    ov[i] = I.B[i].hi * w[0] + I.B[3 + i].hi * w[1] + I.B[6 + i].hi * w[2] + I.C[s[i][0]].hi * v[0] +
-            I.C[s[i][1]].hi * v[1] + I.C[s[i][2]].hi * v[2];
+    ow[i] = A[s[i][0]] * w[0] + A[s[i][1]] * w[1] + A[s[i][2]] * w[2] + B[3 * i] * v[0] + B[3 * i + 1] * v[1] +
+            B[3 * i + 2] * v[2];
+    ov[i] = B[i] * w[0] + B[3 + i] * w[1] + B[6 + i] * w[2] + C[s[i][0]] * v[0] + C[s[i][1]] * v[1] +
+            C[s[i][2]] * v[2];
   }
   return {{ow[0], ow[1], ow[2]}, {ov[0], ov[1], ov[2]}};
 }
@@ -673,6 +681,7 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
         const float arm = c.t(tb + TD_ARMATURE);
         if (arm != 0.0f) D = ff_add(D, ff(arm));
       }
+      D = two_sum(D.hi, D.lo);  // ff_rcp starts from D.hi
       if (!(D.hi > 0.0f)) st |= 2;  // GPB_ST_CHOL_FAIL
       const FF Dinv = ff_rcp(D);
       const FF uf = ff_from_double(u);
@@ -702,8 +711,8 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int j = 0; j < 3; ++j) IA.B[3 * i + j] = ff_fms(IA.B[3 * i + j], Ww[i], Uv[j]);
-        const R ud = ff_mul(uf, Dinv).hi;
-        const SV<R> Ur{{Uw[0].hi, Uw[1].hi, Uw[2].hi}, {Uv[0].hi, Uv[1].hi, Uv[2].hi}};
+        const R ud = ff_f(ff_mul(uf, Dinv));
+        const SV<R> Ur{{ff_f(Uw[0]), ff_f(Uw[1]), ff_f(Uw[2])}, {ff_f(Uv[0]), ff_f(Uv[1]), ff_f(Uv[2])}};
         pa = pA + abi_mul_hi(IA, cb) + scale(Ur, ud);
       }
     } else if (type == 3) {  // floating joint: the FP64 6×6 solve of the FP64 form
@@ -1244,7 +1253,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         ua = ff_fmaf(ffw(c, du + 5), a.v.z, ua);
         const FF xf = ff_mul(ffw(c, du + 6), ff_sub(ffw(c, du + 7), ua));
         x = ff_to_double(xf);
-        xr = xf.hi;
+        xr = ff_f(xf);
       } else {
         const double aw[3] = {double(a.w.x), double(a.w.y), double(a.w.z)};
         const double av[3] = {double(a.v.x), double(a.v.y), double(a.v.z)};

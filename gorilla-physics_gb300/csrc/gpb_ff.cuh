@@ -22,9 +22,11 @@
 //
 // The products-and-sums (ff_fma, ff_fmaf, ff_lin2) return the exact sum of
 // their leading terms plus the rounded sum of the small ones without the
-// final renormalisation: |lo| may reach a few ulp(hi) instead of ½, which
-// every operation here accepts (hi + lo is the same value either way), and it
-// saves 3 of their 12–14 instructions.  ff_add renormalises.
+// final renormalisation: |lo| may reach a few ulp(hi) instead of ½ — after a
+// cancelling subtraction, more than |hi| — which every operation here
+// accepts (hi + lo is the same value either way), and it saves 3 of their
+// 12–14 instructions.  ff_add renormalises.  Where an FP32 approximation of a
+// value is needed, ff_f rounds hi + lo (hi alone can be far off).
 #pragma once
 
 struct alignas(8) FF {
@@ -32,6 +34,8 @@ struct alignas(8) FF {
 };
 
 __device__ __forceinline__ FF ff(float x) { return {x, 0.0f}; }
+// The FP32 value nearest hi + lo.
+__device__ __forceinline__ float ff_f(FF a) { return __fadd_rn(a.hi, a.lo); }
 __device__ __forceinline__ FF ff_neg(FF a) { return {-a.hi, -a.lo}; }
 
 // s + e = a + b exactly (any a, b).
