@@ -103,9 +103,11 @@ enum gpb_precision { GPB_FP64 = 0, GPB_MIXED = 1, GPB_MIXED_REFINED = 2 };
  *   reference uses LU.  The default.
  * GPB_ALGO_ABA: Featherstone's articulated-body algorithm in link coordinates,
  *   O(n) per instance; the same q̈ in exact arithmetic (FP64 results agree with
- *   CRBA to the conditioning bound).  With GPB_MIXED its articulated inertias
- *   stay in FP64 and everything else runs in FP32.  GPB_MIXED_REFINED always
- *   uses CRBA. */
+ *   CRBA to the conditioning bound).  With GPB_MIXED its articulated-inertia
+ *   recursion and the 1-DOF q̈ solve run in double-float (pairs of FP32
+ *   numbers, about 48 bits, on the FP32 pipes) from the FP32-rounded model,
+ *   kinematics and bias forces in FP32, the state, u = τ − Sᵀp^A and a
+ *   floating root's 6×6 solve in FP64.  GPB_MIXED_REFINED always uses CRBA. */
 enum gpb_algorithm { GPB_ALGO_CRBA = 0, GPB_ALGO_ABA = 1 };
 
 /* GPB_HUNT_CROSSLEY: src/contact.rs:260-338 (k = k_p k_h/(k_p+k_h), k_h = 50e3,
