@@ -118,9 +118,9 @@ def test_config_dynamics_fp64(ctx, config, n, model):
 @pytest.mark.parametrize("config,n,model", [(0, 256, 1), (1, 1024, 1), (2, 256, 1), (2, 256, 0),
                                             (3, 128, 1), (3, 128, 0)])
 def test_mixed_aba_error_bound(ctx, algorithm, config, n, model):
-    """MIXED with the articulated-body algorithm (FP64 articulated inertias,
-    FP32 elsewhere): q̈ within 1e-5 of FP64 (relative to max(|q̈|, 1)) on at
-    least 99 % of instances, and within 1e-4 on all of them."""
+    """MIXED with the articulated-body algorithm (double-float articulated
+    inertias, FP32 kinematics): q̈ within 1e-5 of FP64 (relative to
+    max(|q̈|, 1)) on at least 99 % of instances, and within 1e-4 on all of them."""
     if algorithm != "aba":
         pytest.skip("the bound is a property of the ABA form of MIXED")
     M, q0, v0, _ = Model.from_config(config, n, seed=13, contact_model=model)
@@ -138,6 +138,71 @@ def test_mixed_aba_error_bound(ctx, algorithm, config, n, model):
     errs = np.array([rel_err(b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]) for i in range(M.n)])
     assert np.mean(errs <= 1e-5) >= 0.99, (np.mean(errs <= 1e-5), np.quantile(errs, 0.99))
     assert errs.max() <= 1e-4, errs.max()
+
+
+def random_trees(rng, n):
+    """n random trees of 3–9 bodies: revolute joints about general axes with
+    rotated, offset joint frames, revolute joints about ±x/±y/±z with an offset
+    along one axis, prismatic and fixed joints, random parents (branches),
+    inertias with off-diagonal moments and offset centres of mass."""
+    from gpb.model import (WORLD_FRAME, FixedJoint, MechanismState, PrismaticJoint, RevoluteJoint,
+                           RigidBody, SpatialInertia, Transform3D)
+    mechs = []
+    for _ in range(n):
+        joints, bodies = [], []
+        for k in range(int(rng.integers(3, 10))):
+            frame, parent = f"b{k}", WORLD_FRAME if k == 0 else f"b{int(rng.integers(0, k))}"
+            kind = "general" if k == 0 else rng.choice(["general", "principal", "prismatic", "fixed"],
+                                                        p=[0.4, 0.3, 0.2, 0.1])
+            if kind == "principal":
+                axis = np.zeros(3)
+                axis[rng.integers(0, 3)] = rng.choice([-1.0, 1.0])
+                t = np.zeros(3)
+                t[rng.integers(0, 3)] = rng.uniform(-0.6, 0.6)
+                tr = Transform3D(frame, parent, translation=tuple(t))
+            else:
+                quat = rng.normal(size=4)
+                quat /= np.linalg.norm(quat)
+                axis = rng.normal(size=3)
+                axis /= np.linalg.norm(axis)
+                tr = Transform3D(frame, parent, rotation=tuple(quat), translation=tuple(rng.uniform(-0.6, 0.6, 3)))
+            joints.append({"general": RevoluteJoint, "principal": RevoluteJoint,
+                           "prismatic": PrismaticJoint}[kind](tr, axis) if kind != "fixed" else FixedJoint(tr))
+            m = rng.uniform(0.3, 2.0)
+            r = rng.uniform(-0.3, 0.3, 3)
+            a = rng.normal(size=(3, 3))
+            jc = 0.05 * a @ a.T + 0.01 * np.eye(3)
+            bodies.append(RigidBody(SpatialInertia(frame, jc + m * (r @ r * np.eye(3) - np.outer(r, r)), m * r, m)))
+        mechs.append(MechanismState(joints, bodies))
+    return Model.from_mechanisms(mechs)
+
+
+def test_general_trees(ctx, algorithm):
+    """Random trees with every joint kind and transform the chain
+    configurations do not have (general axes and joint rotations, offsets
+    along several axes, prismatic and fixed joints, branches): FP64 against
+    the oracle, and MIXED ABA (its general-rotation, general-shift, prismatic
+    and fixed-joint double-float paths) against FP64."""
+    rng = np.random.default_rng(44)
+    M = random_trees(rng, 512)
+    qo, vo, _ = M.offsets()
+    q0 = rng.uniform(-math.pi, math.pi, qo[-1])
+    v0 = rng.normal(size=vo[-1])
+    tau = rng.normal(size=vo[-1])
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    a = B.dynamics_continuous(tau, precision=gpb.FP64)
+    for i in range(0, M.n, 8):
+        ref, st = oracle.dynamics(M, i, q0[qo[i]:qo[i + 1]], v0[vo[i]:vo[i + 1]], tau[vo[i]:vo[i + 1]])
+        assert st == 0
+        assert rel_err(a[vo[i]:vo[i + 1]], ref) <= 1e-9, i
+    if algorithm != "aba":
+        return
+    b = B.dynamics_continuous(tau, precision=gpb.MIXED)
+    errs = np.array([rel_err(b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]) for i in range(M.n)])
+    assert np.mean(errs <= 1e-5) >= 0.99, (np.mean(errs <= 1e-5), np.quantile(errs, 0.99))
+    assert errs.max() <= 1e-4, errs.max()
+    assert np.all(B.status() == 0)
 
 
 def test_mixed_precision_error(ctx):
