@@ -7,8 +7,8 @@ semi-implicit Euler at dt = 5e-4.  One bench "step" is one integrator step of
 every instance; the timed region runs `--steps` of them in one persistent
 launch.  Four forms are timed: FP64 through the reference's route (CRBA +
 solve), FP64 articulated-body algorithm, mixed precision (articulated-body
-algorithm with FP64 articulated inertias) and CRBA with FP64 iterative
-refinement.  `value` is the fastest form whose per-step q̈ stays within 1e-5
+algorithm with FP32 kinematics and double-float articulated inertias) and
+CRBA with FP64 iterative refinement.  `value` is the fastest form whose per-step q̈ stays within 1e-5
 of FP64 CRBA on ≥ 99 % of instances, at the initial and the final states.
 
 `--impl reference` times the CPU restatement of the reference's `simulate`
@@ -396,7 +396,7 @@ def run_gpu(args):
 
     WORK = {"fp64_crba": "CRBA + RNEA + Cholesky flops (gpb.flops.model_flops)",
             "fp64": "articulated-body algorithm flops (gpb.flops.aba_model_flops)",
-            "mixed": "FP64 share of the mixed articulated-body algorithm (gpb.flops.aba_model_flops(mixed=True))",
+            "mixed": "FP64 share of the mixed articulated-body algorithm (gpb.flops.aba_model_flops(mixed=True))",  # configurations without the instruction count
             "refined": "CRBA-equivalent flops (the FP64 residual is a part of them)"}
     # The mixed form runs its precision-critical recursion in double-float on the
     # FP32 pipes: no single pipe is near its peak, and its roofline is the SM's

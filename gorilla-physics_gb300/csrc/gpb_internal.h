@@ -74,7 +74,7 @@ __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, 
   s.I = o; o += 12 * nb;  // world inertia (10) or, in link coordinates, (Rrel, t) (12)
   s.F = o; o += 6 * nb;
   s.C = o; o += 10 * nb;  // link coordinates: composite inertia accumulated from branches
-  s.AI = o; o += 21 * nb; // articulated-body algorithm: articulated inertias (FP64)
+  s.AI = o; o += 21 * nb; // articulated-body algorithm: articulated inertias (FP64 or double-float)
   s.DU = o; o += 11 * nv; // articulated-body algorithm: U, 1/D, u per DOF (FP64)
   s.RF = o; o += 12 * nb; // articulated-body algorithm: (Rrel, t) in the sweep precision
   const int nT = (nv + 3) / 4;  // mass matrix in 4x4 tiles, n padded to 4 nT

@@ -963,7 +963,7 @@ struct EvalFP64 {
     return lane_dynamics<double, double>(c, q, v, t, ht, x, cf, want_cf);
   }
 };
-struct EvalMixed {  // CRBA: FP32 sweeps and fill, FP64 Cholesky when n > 12; ABA: FP64 articulated inertias
+struct EvalMixed {  // CRBA: FP32 sweeps and fill, FP64 Cholesky when n > 12; ABA: double-float articulated inertias
   LaneCtx<float> c;
   int algo;
   __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
