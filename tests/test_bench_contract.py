@@ -1,0 +1,56 @@
+"""bench.py's JSON contract on CPU: the committed headline line has every key
+and a consistent roofline, the reference arm runs here and prints its line, and
+the committed ncu tables hold what bench.py reads from them."""
+
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+KEYS = ["metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+        "vs_baseline", "dtype", "data", "config", "gpu_launches", "roofline", "cpu_baseline", "e2e", "clocks"]
+
+
+def test_committed_headline_line():
+    d = json.loads((ROOT / "profiles" / "bench_serial-chain_65536.json").read_text())
+    assert [k for k in KEYS if k not in d] == []
+    assert d["config"]["workload"].startswith("serial-chain")
+    r = d["roofline"]
+    for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
+        assert k in r
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) <= 1e-9 * r["frac"]
+    assert 0.0 < r["frac"] < 1.5
+    assert d["gpu_launches"] >= 1
+    assert set(d["e2e"]) >= {"value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"}
+    assert d["e2e"]["h2d_bytes_per_step"] > 0 and d["e2e"]["d2h_bytes_per_step"] > 0
+    assert set(d["cpu_baseline"]) >= {"value", "unit", "cores", "kind", "sample"}
+    assert d["clocks"]["reasons"] == [] or "sw_power_cap" in d["clocks"]["reasons"]
+    # the headline is the fastest form within the q̈ bar
+    for name, m in d["modes"].items():
+        err = m["qdd_rel_err_vs_fp64_crba"] or {}
+        if all(e["frac_le_1e-5"] >= 0.99 for e in err.values()):
+            assert m["value"] <= d["value"] * (1 + 1e-12), name
+
+
+def test_ncu_tables_hold_what_bench_reads():
+    t = json.loads((ROOT / "profiles" / "dram_traffic_per_instance_step.json").read_text())
+    m = t["serial-chain"]["mixed"]
+    assert m["dram_bytes_per_instance_step"] > 0 and m["warp_instructions_per_instance_step"] > 0
+    assert "capture" in m
+    v = json.loads((ROOT / "profiles" / "vstep_work.json").read_text())
+    assert v["fp64_flops_per_instance_step"] > 0 and "source" in v
+    c = json.loads((ROOT / "profiles" / "collision_work.json").read_text())
+    assert c["gripper"]["mean_flops_per_evaluation"] > 0
+
+
+def test_reference_arm_prints_its_line():
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "1"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    for k in ("metric", "value", "unit", "higher_is_better", "config", "cpu_baseline", "e2e"):
+        assert k in line
+    assert line["value"] > 0 and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
