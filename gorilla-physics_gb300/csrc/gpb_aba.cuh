@@ -784,6 +784,12 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
   const bool wide = contacts || sizeof(R) == 8;  // FP64 joint transforms
   const V zero{R(0), R(0), R(0)};
   V pw_ = zero, pv_ = zero;                  // parent velocity (chain carry)
+  // The mixed form of a contact mechanism propagates its body velocities in
+  // FP64: the regularised friction divides the contact point's tangential
+  // velocity by 1e-3, so an FP32 velocity recursion (errors ~1e-7 of the body
+  // speeds along a leg) would become a ~1e-4 error in the friction force.
+  const bool dvel = sizeof(R) == 4 && contacts;
+  VD pwd_{0.0, 0.0, 0.0}, pvd_{0.0, 0.0, 0.0};  // its FP64 chain carry
   VD ppos{0.0, 0.0, 0.0};
   M3<double> pR = eye3<double>();            // parent world pose (contacts only)
   int st = 0;
@@ -793,17 +799,24 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     const int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
     const uint32_t fl = w1 & 255;
     V om = zero, vl = zero;
+    VD omd{0.0, 0.0, 0.0}, vld{0.0, 0.0, 0.0};
     VD posw{0.0, 0.0, 0.0};
     M3<double> Rw = eye3<double>();
     if (parent == b && parent != 0) {
       om = pw_;
       vl = pv_;
+      omd = pwd_;
+      vld = pvd_;
       posw = ppos;
       Rw = pR;
     } else if (parent != 0) {
       const int pb = parent - 1;
       om = {c.r(c.L.V + 6 * pb), c.r(c.L.V + 6 * pb + 1), c.r(c.L.V + 6 * pb + 2)};
       vl = {c.r(c.L.V + 6 * pb + 3), c.r(c.L.V + 6 * pb + 4), c.r(c.L.V + 6 * pb + 5)};
+      if (dvel) {
+        omd = {c.d(c.L.VW + 6 * pb), c.d(c.L.VW + 6 * pb + 1), c.d(c.L.VW + 6 * pb + 2)};
+        vld = {c.d(c.L.VW + 6 * pb + 3), c.d(c.L.VW + 6 * pb + 4), c.d(c.L.VW + 6 * pb + 5)};
+      }
       if (contacts) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) Rw.a[k] = c.d(c.L.X + 12 * pb + k);
@@ -891,19 +904,39 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     }
     const V t{R(td.x), R(td.y), R(td.z)};
     // velocity: v = X v_p + S q̇ ; bias acceleration c = v ×m (S q̇)
-    vl = mulT(Rr, vl + cross(om, t));
-    om = mulT(Rr, om);
     V jw = zero, jv = zero;
-    if (type == 1 || type == 2) {
-      const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
-      if (type == 1) jw = ax * R(v[vo]);
-      else jv = ax * R(v[vo]);
-    } else if (type == 3) {
-      jw = {R(v[vo]), R(v[vo + 1]), R(v[vo + 2])};
-      jv = {R(v[vo + 3]), R(v[vo + 4]), R(v[vo + 5])};
+    if (dvel) {  // FP64 recursion, rounded for the FP32 bias terms
+      vld = mulT(Rd, vld + cross(omd, td));
+      omd = mulT(Rd, omd);
+      VD jwd{0.0, 0.0, 0.0}, jvd{0.0, 0.0, 0.0};
+      if (type == 1 || type == 2) {
+        const VD axd{c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
+        if (type == 1) jwd = axd * v[vo];
+        else jvd = axd * v[vo];
+      } else if (type == 3) {
+        jwd = {v[vo], v[vo + 1], v[vo + 2]};
+        jvd = {v[vo + 3], v[vo + 4], v[vo + 5]};
+      }
+      omd = omd + jwd;
+      vld = vld + jvd;
+      om = {R(omd.x), R(omd.y), R(omd.z)};
+      vl = {R(vld.x), R(vld.y), R(vld.z)};
+      jw = {R(jwd.x), R(jwd.y), R(jwd.z)};
+      jv = {R(jvd.x), R(jvd.y), R(jvd.z)};
+    } else {
+      vl = mulT(Rr, vl + cross(om, t));
+      om = mulT(Rr, om);
+      if (type == 1 || type == 2) {
+        const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
+        if (type == 1) jw = ax * R(v[vo]);
+        else jv = ax * R(v[vo]);
+      } else if (type == 3) {
+        jw = {R(v[vo]), R(v[vo + 1]), R(v[vo + 2])};
+        jv = {R(v[vo + 3]), R(v[vo + 4]), R(v[vo + 5])};
+      }
+      om = om + jw;
+      vl = vl + jv;
     }
-    om = om + jw;
-    vl = vl + jv;
     const SV<R> cb{cross(om, jw), cross(om, jv) + cross(vl, jw)};
     // bias force p = v ×* I v − f_contact (body frame)
     SI<R> I;
@@ -959,11 +992,14 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
             const V nb{R(nbd.x), R(nbd.y), R(nbd.z)};
             const V app = rad > R(0) ? loc - nb * rad : loc;  // application point (body frame)
             const VD appd = radd > 0.0 ? locd - nbd * radd : locd;
-            // a floating root's body velocity is the state itself: read it unrounded
+            // a floating root's body velocity is the state itself: read it
+            // unrounded; the mixed form's other bodies carry FP64 velocities
             const bool root6 = type == 3 && parent == 0;
-            const VD vld = root6 ? VD{v[vo + 3], v[vo + 4], v[vo + 5]} : VD{double(vl.x), double(vl.y), double(vl.z)};
-            const VD omd = root6 ? VD{v[vo], v[vo + 1], v[vo + 2]} : VD{double(om.x), double(om.y), double(om.z)};
-            const VD vd = vld + cross(omd, appd);
+            const VD vlc = root6 ? VD{v[vo + 3], v[vo + 4], v[vo + 5]}
+                                 : (dvel ? vld : VD{double(vl.x), double(vl.y), double(vl.z)});
+            const VD omc = root6 ? VD{v[vo], v[vo + 1], v[vo + 2]}
+                                 : (dvel ? omd : VD{double(om.x), double(om.y), double(om.z)});
+            const VD vd = vlc + cross(omc, appd);
             const VD fbd = contact_force<double>(c.model, pen, nbd, vd, c.cdd(cd + 3), c.cdd(cd + 5), alh, mu);
             const V fb{R(fbd.x), R(fbd.y), R(fbd.z)};
             wc.w = wc.w - cross(appd, fbd);
@@ -982,10 +1018,12 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       const int uslot = (int)((w1 >> W1_CUBOID_SHIFT) & 15u);
       if (uslot && c.nu > 1) {  // cuboid record: world pose, world twist about the origin
         const bool root6 = type == 3 && parent == 0;
-        const VD omd = root6 ? VD{v[vo], v[vo + 1], v[vo + 2]} : VD{double(om.x), double(om.y), double(om.z)};
-        const VD vld = root6 ? VD{v[vo + 3], v[vo + 4], v[vo + 5]} : VD{double(vl.x), double(vl.y), double(vl.z)};
-        const VD omw = mul(Rw, omd);
-        store_cuboid(c, uslot - 1, b, Rw, posw, omw, mul(Rw, vld) - cross(omw, posw));
+        const VD omc = root6 ? VD{v[vo], v[vo + 1], v[vo + 2]}
+                             : (dvel ? omd : VD{double(om.x), double(om.y), double(om.z)});
+        const VD vlc = root6 ? VD{v[vo + 3], v[vo + 4], v[vo + 5]}
+                             : (dvel ? vld : VD{double(vl.x), double(vl.y), double(vl.z)});
+        const VD omw = mul(Rw, omc);
+        store_cuboid(c, uslot - 1, b, Rw, posw, omw, mul(Rw, vlc) - cross(omw, posw));
       }
     }
     // records for the inward and second outward passes: (Rrel, t) in R (the
@@ -1024,6 +1062,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       if (sizeof(R) == 8) store_abi(c, c.L.AI + ABI_D * b, ABI{});
       else store_abi_ff(c, c.L.AI + ABI_D * b, ABIF{});
       store_sv(c, c.L.V + 6 * b, vb);
+      if (dvel) store_svd(c, c.L.VW + 6 * b, SV<double>{omd, vld});
       if (contacts) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) c.d(c.L.X + 12 * b + k) = Rw.a[k];
@@ -1034,6 +1073,8 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     }
     pw_ = om;
     pv_ = vl;
+    pwd_ = omd;
+    pvd_ = vld;
     ppos = posw;
     pR = Rw;
   }

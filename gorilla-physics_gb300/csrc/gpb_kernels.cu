@@ -1122,8 +1122,12 @@ struct EvalOf<2> {
 
 #include "gpb_coop.cuh"
 
+// The mixed form at three blocks per SM (168 registers per thread): the
+// compiler's own allocation for it otherwise grows to 255 with the FP64
+// velocity recursion of contact mechanisms, which costs the chains
+// (lane-per-instance code without contacts) their spare occupancy.
 template <int PREC>
-__global__ void __launch_bounds__(128) simulate_kernel(DeviceBatch b, StepParams p) {
+__global__ void __launch_bounds__(128, PREC == 1 ? 3 : 1) simulate_kernel(DeviceBatch b, StepParams p) {
   const int lane = threadIdx.x & 31;
   // packs [0, ncoop): one whole block per pack (large mechanisms, largest first)
   if (PREC != 2 && p.ncoop > 0) {
