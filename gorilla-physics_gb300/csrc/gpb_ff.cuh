@@ -9,7 +9,8 @@
 // The building blocks are the published error-free transformations:
 //   two_sum       Knuth, TAOCP vol. 2 §4.2.2 (s + e = a + b exactly, 6 adds);
 //   fast_two_sum  Dekker 1971 (the same for |a| ≥ |b|, 3 adds);
-//   two_prod      with a fused multiply-add: p + e = a·b exactly (2 ops);
+//   the exact product with a fused multiply-add: p = a·b rounded,
+//                 e = fma(a, b, −p), p + e = a·b exactly (2 ops);
 // composed as in Dekker, "A floating-point technique for extending the
 // available precision" (Numer. Math. 18, 1971) and Hida, Li & Bailey's
 // double-double library (2001): the sum adds the low parts after an exact
@@ -50,11 +51,6 @@ __device__ __forceinline__ FF fast_two_sum(float a, float b) {
   const float s = __fadd_rn(a, b);
   return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
-// p + e = a·b exactly.
-__device__ __forceinline__ FF two_prod(float a, float b) {
-  const float p = __fmul_rn(a, b);
-  return {p, __fmaf_rn(a, b, -p)};
-}
 
 __device__ __forceinline__ FF ff_add(FF a, FF b) {
   const FF s = two_sum(a.hi, b.hi);
@@ -62,13 +58,6 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
 }
 __device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, ff_neg(b)); }
 
-// a·f for an FP32 factor f (the product of the low part rounds once).
-__device__ __forceinline__ FF ff_mulf(FF a, float f) {
-  const float p = __fmul_rn(a.hi, f);
-  float e = __fmaf_rn(a.hi, f, -p);
-  e = __fmaf_rn(a.lo, f, e);
-  return fast_two_sum(p, e);
-}
 __device__ __forceinline__ FF ff_mul(FF a, FF b) {
   const float p = __fmul_rn(a.hi, b.hi);
   float e = __fmaf_rn(a.hi, b.hi, -p);
