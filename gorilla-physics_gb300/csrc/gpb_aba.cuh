@@ -584,6 +584,15 @@ template <typename R>
 __device__ __forceinline__ SV<R> sv_r(const SV<double>& s) {
   return {{R(s.w.x), R(s.w.y), R(s.w.z)}, {R(s.v.x), R(s.v.y), R(s.v.z)}};
 }
+// Row of the FP64 bias forces of a contact mechanism: F itself in the FP64
+// form; in the mixed form the separate region FD, since F holds the FP32 bias
+// forces of the pack's lanes without contacts and an FP32 row fills the first
+// half of the bytes of the FP64 row of the same index (the FP64 elements of
+// lanes 0-15).
+template <typename R>
+__device__ __forceinline__ int fd_row(const LaneCtx<R>& c) {
+  return sizeof(R) == 8 ? c.L.F : c.L.FD;
+}
 template <typename R>
 __device__ __forceinline__ SV<double> load_svd(const LaneCtx<R>& c, int base) {
   return {{c.d(base), c.d(base + 1), c.d(base + 2)}, {c.d(base + 3), c.d(base + 4), c.d(base + 5)}};
@@ -621,7 +630,7 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
     SV<double> pAd;
     SV<R> pA;
     if (contacts) {
-      pAd = load_svd(c, c.L.F + 6 * b);
+      pAd = load_svd(c, fd_row(c) + 6 * b);
       if (ctarget == b) pAd = pAd + sv_d(carryP);
       pA = sv_r<R>(pAd);
     } else {
@@ -761,7 +770,7 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
         carryP = fp;
         ctarget = pb;
       } else {
-        if (contacts) store_svd(c, c.L.F + 6 * pb, load_svd(c, c.L.F + 6 * pb) + sv_d(fp));
+        if (contacts) store_svd(c, fd_row(c) + 6 * pb, load_svd(c, fd_row(c) + 6 * pb) + sv_d(fp));
         else store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
         ctarget = -1;
       }
@@ -1055,7 +1064,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       c.r(c.L.RF + 12 * b + 11) = t.z;
     }
     store_sv(c, c.L.A + 6 * b, cb);
-    if (contacts) store_svd(c, c.L.F + 6 * b, sv_d(p) + wc);  // bias forces of contact mechanisms: FP64
+    if (contacts) store_svd(c, fd_row(c) + 6 * b, sv_d(p) + wc);  // bias forces of contact mechanisms: FP64
     else store_sv(c, c.L.F + 6 * b, p);
     if (fl & BF_BRANCH) {
       // accumulator for children other than b+1
@@ -1083,7 +1092,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     st |= lane_cuboid_pairs(c);
     for (int b = 0; b < c.nb; ++b) {
       const int uslot = (int)((c.w(2 * b + 1) >> W1_CUBOID_SHIFT) & 15u);
-      if (uslot) store_svd(c, c.L.F + 6 * b, load_svd(c, c.L.F + 6 * b) - cuboid_wrench_body(c, uslot - 1));
+      if (uslot) store_svd(c, fd_row(c) + 6 * b, load_svd(c, fd_row(c) + 6 * b) - cuboid_wrench_body(c, uslot - 1));
     }
   }
   // ---- pass 2 (inward): articulated inertias and bias forces --------------
@@ -1104,7 +1113,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       SV<double> pAd;  // FP64 copy (contact mechanisms) for u
       SV<R> pA;
       if (contacts) {
-        pAd = load_svd(c, c.L.F + 6 * b);
+        pAd = load_svd(c, fd_row(c) + 6 * b);
         if (ctarget == b) pAd = pAd + sv_d(carryP);
         pA = sv_r<R>(pAd);
       } else {
@@ -1252,7 +1261,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
           carryP = fp;
           ctarget = pb;
         } else {
-          if (contacts) store_svd(c, c.L.F + 6 * pb, load_svd(c, c.L.F + 6 * pb) + sv_d(fp));
+          if (contacts) store_svd(c, fd_row(c) + 6 * pb, load_svd(c, fd_row(c) + 6 * pb) + sv_d(fp));
           else store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
           ctarget = -1;
         }

@@ -713,6 +713,20 @@ extern "C" int gpb_dynamics_static(gpb_batch* b, const double* q, const double* 
                                  std::to_string((int64_t)GPB_STATIC_SCRATCH_BYTES) +
                                  " (use gpb_dynamics, or a smaller batch)");
   CUDA_TRY(cudaSetDevice(b->ctx->device));
+  // A host pointer would make the kernel fault: accept device or managed memory only.
+  const void* bufs[4] = {q, v, qdd, tau};
+  const char* names[4] = {"q", "v", "qdd", "tau"};
+  for (int k = 0; k < 4; ++k) {
+    if (!bufs[k]) continue;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, bufs[k]) != cudaSuccess) {
+      cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+      return fail(GPB_E_INVAL, std::string("gpb_dynamics_static: ") + names[k] + " is not a CUDA pointer");
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+      return fail(GPB_E_INVAL, std::string("gpb_dynamics_static: ") + names[k] +
+                                   " must be device or managed memory");
+  }
   cudaStream_t s = stream ? (cudaStream_t)stream : b->ctx->stream;
   CUDA_TRY(launch_dynamics_static(b->dev(), b->ctx->device, b->scratch_words, precision, q, v, tau,
                                   qdd, s));

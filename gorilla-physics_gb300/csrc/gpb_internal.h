@@ -62,7 +62,7 @@ struct PackDesc {
 // Scratch sub-array offsets (rows of 8-byte words; R-typed arrays use the same
 // row pitch so that the float and double kernels share one layout).
 struct ScratchLayout {
-  int32_t X, V, A, S, I, F, C, AI, DU, RF, M, D, rhs, q0, v0, qs, vs, facc, tau, cf, U, VW, total;
+  int32_t X, V, A, S, I, F, C, AI, DU, RF, M, D, rhs, q0, v0, qs, vs, facc, tau, cf, U, VW, FD, total;
 };
 __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, int nc, int nu) {
   ScratchLayout s;
@@ -91,6 +91,11 @@ __host__ __device__ inline ScratchLayout scratch_layout(int nb, int nq, int nv, 
   s.U = o; o += nu > 1 ? UREC_D * nu : 0;  // cuboid records (pairs need two)
   // mixed articulated-body algorithm of contact mechanisms: FP64 body velocities of branch bodies
   s.VW = o; o += (nc > 0 || nu > 1) ? 6 * nb : 0;
+  // mixed articulated-body algorithm of contact mechanisms: FP64 bias forces.  They
+  // cannot share F with the FP32 bias forces of the pack's other lanes: an FP32
+  // row fills the first half of the bytes of the FP64 row of the same index,
+  // i.e. the FP64 elements of lanes 0-15.
+  s.FD = o; o += (nc > 0 || nu > 1) ? 6 * nb : 0;
   s.total = o;
   return s;
 }

@@ -1414,7 +1414,8 @@ cudaError_t launch_gather(const int64_t* map, int64_t slots, const double* src, 
 static __device__ __align__(256) double gpb_static_scratch[GPB_STATIC_SCRATCH_BYTES / sizeof(double)];
 
 // Host-side stand-in of the array above is not a device address: the address a
-// kernel may use is looked up once per device, with that device current.
+// kernel may use is looked up once per device, with that device current, and
+// kept for the life of the process (it does not survive a cudaDeviceReset).
 constexpr int kMaxDevices = 64;
 static std::mutex g_static_mu;
 static double* g_static_ptr[kMaxDevices] = {};

@@ -248,9 +248,21 @@ int gpb_dynamics(gpb_batch* batch, const double* tau, int precision, double* qdd
  * The kernel runs asynchronously on `stream` (a cudaStream_t; NULL = the
  * batch's context stream); read qdd after synchronising that stream.  The first
  * call on a device looks up the array's device address, so make that first call
- * before any stream capture.  All calls share the one array: calls whose
- * kernels overlap on the GPU race, so order them on one stream.  No state is
- * carried from one call to the next.
+ * before any stream capture.  The address is kept for the life of the process:
+ * do not call this entry point again on a device after cudaDeviceReset (or any
+ * other teardown of that device's primary context).  All calls share the one
+ * array: calls whose kernels overlap on the GPU race, so order them on one
+ * stream.  No state is carried from one call to the next.
+ *
+ * The kernel also ORs its per-instance status bits into the batch's status
+ * array (gpb_batch_status), on `stream`.  Every other entry point of the batch
+ * works on the context stream, so with a non-NULL `stream` the caller must
+ * order the two: synchronise `stream` before gpb_batch_status,
+ * gpb_batch_clear_status, gpb_step or gpb_simulate on the same batch, and do not
+ * let this call overlap one of those.
+ *
+ * q, v, qdd (and tau when not NULL) must be device (or managed) memory: a host
+ * pointer is rejected with GPB_E_INVAL before anything is launched.
  */
 #define GPB_STATIC_SCRATCH_BYTES (16u << 20)
 int gpb_dynamics_static(gpb_batch* batch, const double* q, const double* v, const double* tau,

@@ -140,6 +140,60 @@ def test_mixed_aba_error_bound(ctx, algorithm, config, n, model):
     assert errs.max() <= 1e-4, errs.max()
 
 
+def _pack_kinds(M):
+    """Contact / no-contact kinds of the lanes of every pack of 32, in the
+    library's pack order (instances sorted by DOF, bodies and contacts, largest
+    first; ties keep their order within a topology)."""
+    qo, vo, co = M.offsets()
+    nb = np.diff(M.joint_offset)
+    nv, nc = np.diff(vo), np.diff(co)
+    order = sorted(range(M.n), key=lambda i: (-nv[i], -nb[i], -nc[i]))
+    return [{bool(nc[i] > 0) for i in order[k:k + 32]} for k in range(0, M.n, 32)]
+
+
+@pytest.mark.parametrize("precision", [gpb.FP64, gpb.MIXED, gpb.MIXED_REFINED])
+def test_mixed_contact_batches(ctx, algorithm, precision):
+    """Quadrupeds (contacts) batched with serial chains (none), so that packs
+    hold both kinds: every instance's q̈ is bit-identical to the one it gets in
+    a batch of its own kind (a lane reads and writes nothing of its
+    neighbours), MIXED with the articulated-body algorithm stays within 1e-4 of
+    FP64 (relative to max(|q̈|, 1)), MIXED_REFINED within 1e-6, and no status
+    bit is set.  A mixed pack once let the FP32 bias forces of its
+    chain lanes overwrite the FP64 bias forces of its contact lanes."""
+    if algorithm == "aba" and precision == gpb.MIXED_REFINED:
+        pytest.skip("MIXED_REFINED always uses CRBA")
+    M3, q3, v3, _ = Model.from_config(3, 75, seed=31)
+    M1, q1, v1, _ = Model.from_config(1, 600, seed=32)
+    qo3, _, _ = M3.offsets()
+    rng = np.random.default_rng(31)
+    q3 = q3.copy()
+    for i in range(M3.n):  # feet in the ground
+        q3[qo3[i] + 6] = rng.uniform(0.38, 0.45)
+    M = Model.concat([M3, M1])
+    q0, v0 = np.concatenate([q3, q1]), np.concatenate([v3, v1])
+    tau = rng.normal(size=v0.size)
+    assert sum(len(k) == 2 for k in _pack_kinds(M)) >= 2  # packs that straddle the kinds
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    mix = B.dynamics_continuous(tau, precision=precision)
+    st = B.status()
+    ref = B.dynamics_continuous(tau, precision=gpb.FP64)
+    n3 = int(v3.size)
+    for Mk, qk, vk, sl in ((M3, q3, v3, slice(0, n3)), (M1, q1, v1, slice(n3, None))):
+        A = Batch(Mk, ctx)
+        A.update(qk, vk)
+        alone = A.dynamics_continuous(tau[sl], precision=precision)
+        np.testing.assert_array_equal(mix[sl], alone)
+        A.close()
+    # MIXED with CRBA is the FP32 mass-matrix form, limited by cond(H)·ε32: no bound
+    bound = {gpb.FP64: 0.0, gpb.MIXED: 1e-4 if algorithm == "aba" else None, gpb.MIXED_REFINED: 1e-6}[precision]
+    if bound is not None:
+        _, vo, _ = M.offsets()
+        errs = np.array([rel_err(mix[vo[i]:vo[i + 1]], ref[vo[i]:vo[i + 1]]) for i in range(M.n)])
+        assert errs.max() <= bound, (errs.max(), int(np.argmax(errs)))
+    assert np.all(st == 0)
+
+
 def random_trees(rng, n):
     """n random trees of 3–9 bodies: revolute joints about general axes with
     rotated, offset joint frames, revolute joints about ±x/±y/±z with an offset

@@ -5,9 +5,10 @@ dynamics (a hard real-time loop, or a host that hands out GPU memory through
 its own pool): the caller passes device buffers for q, v, τ and q̈, and the
 kernel's working memory is a fixed array inside the library.  These tests call
 it through the C ABI with device buffers and check it against gpb_dynamics (the
-allocating entry point) twice in a row — the second call runs on whatever the
-first left in the shared array.  The file is named so that pytest collects it
-last.
+allocating entry point) on three calls in a row: the state of the first call,
+a perturbed state, then the first state again — so the later calls run on the
+different words the previous call left in the shared array.  The file is named
+so that pytest collects it last.
 """
 
 import ctypes as C
@@ -30,7 +31,7 @@ def _dev(a):
 
 
 @pytest.mark.parametrize("config,n", [(0, 96), (1, 64), (2, 64), (3, 48)])
-@pytest.mark.parametrize("precision", [gpb.FP64, gpb.MIXED])
+@pytest.mark.parametrize("precision", [gpb.FP64, gpb.MIXED, gpb.MIXED_REFINED])
 def test_static_scratch_matches_allocating_path(ctx, config, n, precision):
     import torch
 
@@ -42,13 +43,24 @@ def test_static_scratch_matches_allocating_path(ctx, config, n, precision):
         for i in range(n):
             q0[qo[i] + 6] = rng.uniform(0.0, 0.4) if config == 2 else rng.uniform(0.38, 0.45)
     tau = rng.normal(size=v0.size)
+    # a second state: every joint coordinate and velocity moved (quaternions
+    # of floating joints are left as they are, so they stay unit)
+    q1, v1, tau1 = q0.copy(), v0 + rng.normal(scale=0.5, size=v0.size), -0.5 * tau
+    for i in range(n):
+        nq = qo[i + 1] - qo[i]
+        if nq == vo[i + 1] - vo[i]:
+            q1[qo[i]:qo[i + 1]] += rng.uniform(-0.3, 0.3, nq)
+        else:
+            q1[qo[i] + 4:qo[i + 1]] += rng.uniform(-0.02, 0.02, nq - 4)
     B = Batch(M, ctx)
-    B.update(q0, v0)
-    ref = B.dynamics_continuous(tau, precision=precision)
-    qd, vd, td = _dev(q0), _dev(v0), _dev(tau)
+    refs = []
+    for q, v, t in ((q0, v0, tau), (q1, v1, tau1)):
+        B.update(q, v)
+        refs.append((q, v, t, B.dynamics_continuous(t, precision=precision)))
     L = _abi.lib()
     stream = torch.cuda.current_stream().cuda_stream
-    for call in range(2):
+    for call, (q, v, t, ref) in enumerate((refs[0], refs[1], refs[0])):
+        qd, vd, td = _dev(q), _dev(v), _dev(t)
         out = torch.full((B.nv,), float("nan"), dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
         rc = L.gpb_dynamics_static(B.h, qd.data_ptr(), vd.data_ptr(), td.data_ptr(), precision,
@@ -61,6 +73,21 @@ def test_static_scratch_matches_allocating_path(ctx, config, n, precision):
             err = np.max(np.abs(g - r)) / max(np.max(np.abs(r)), 1.0)
             assert err <= TOL, (call, i, err)
     assert np.all(B.status() == 0)
+    B.close()
+
+
+def test_static_scratch_rejects_host_buffers(ctx):
+    """A host pointer is refused with GPB_E_INVAL before any launch (a kernel
+    given it would fault)."""
+    M, q0, v0, _ = Model.from_config(0, 8, seed=3)
+    B = Batch(M, ctx)
+    qd, vd = _dev(q0), _dev(v0)
+    out = _dev(np.zeros(v0.size))
+    host = np.zeros(v0.size)
+    L = _abi.lib()
+    rc = L.gpb_dynamics_static(B.h, qd.data_ptr(), host.ctypes.data, None, gpb.FP64, out.data_ptr(), None)
+    assert rc == _abi.GPB_E_INVAL
+    assert "device or managed memory" in L.gpb_last_error().decode()
     B.close()
 
 
