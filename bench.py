@@ -257,18 +257,26 @@ def qdd_error(B, gpb, precision, algorithm, where):
     B.set_algorithm(algorithm)
     b = B.dynamics_continuous(None, precision=precision)
     vo = B.v_offset
-    err = []
+    err, rel = [], []
     for i in np.nonzero(ok)[0]:
         x, y = b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]
-        e = np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1.0) if y.size else 0.0
+        d = np.max(np.abs(x - y)) if y.size else 0.0
+        m = np.max(np.abs(y)) if y.size else 0.0
+        e = d / max(m, 1.0)
+        r = d / m if m > 0 else (0.0 if d == 0 else np.inf)
         err.append(e if np.isfinite(e) else np.inf)
-    err = np.asarray(err)
+        rel.append(r if np.isfinite(r) else np.inf)
+    err, rel = np.asarray(err), np.asarray(rel)
     fin = err[np.isfinite(err)]
+    rfin = rel[np.isfinite(rel)]
     return {"max": float(fin.max()) if fin.size else None,
             "p99": float(np.quantile(err, 0.99)), "median": float(np.median(err)),
             "frac_le_1e-5": float(np.mean(err <= 1e-5)), "nonfinite": int(np.sum(~np.isfinite(err))),
             "instances": int(err.size), "state": where,
-            "norm": "max|Δq̈| / max(max|q̈_fp64,crba|, 1) per instance"}
+            "norm": "max|Δq̈| / max(max|q̈_fp64,crba|, 1) per instance",
+            "relative": {"max": float(rfin.max()) if rfin.size else None,
+                         "p99": float(np.quantile(rel, 0.99)), "frac_le_1e-5": float(np.mean(rel <= 1e-5)),
+                         "norm": "max|Δq̈| / max|q̈_fp64,crba| per instance (no floor)"}}
 
 
 def run_gpu(args):
@@ -359,13 +367,13 @@ def run_gpu(args):
     for name in errs:
         prec, algo, _ = MODES[name]
         errs[name]["initial"] = qdd_error(B, gpb, prec, algo, "the configuration's initial states")
-    # headline: the fastest form that meets the stated bound (≤ 1e-5 on ≥ 99 % of
-    # instances at both states); the FP64 forms are exact to round-off
+    # headline: the fastest form that meets the stated bound (every instance
+    # within 1e-5 at both states); the FP64 forms are exact to round-off
     head_name = max([p for p in precs if p.startswith("fp64")] or precs[:1],
                     key=lambda n: results[n]["done"] / results[n]["kernel_ms"])
     for name in ["mixed", "refined"]:
         e = errs.get(name)
-        if name in results and e and all(x["frac_le_1e-5"] >= 0.99 for x in e.values()):
+        if name in results and e and all(x["frac_le_1e-5"] == 1.0 for x in e.values()):
             if results[name]["kernel_ms"] < results[head_name]["kernel_ms"]:
                 head_name = name
     # e2e through the public API: host (pinned) state in, K steps, state out

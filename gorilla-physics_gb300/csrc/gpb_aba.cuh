@@ -473,6 +473,136 @@ __device__ __forceinline__ SV<float> abi_mul_hi(const ABIF& I, const SV<float>& 
   return {{ow[0], ow[1], ow[2]}, {ov[0], ov[1], ov[2]}};
 }
 
+// ---- double-float bias forces (GPB_MIXED) ----------------------------------
+// The bias force p = v ×* I v of each body and the inward recursion
+// p^a = p^A + I^a c + U D⁻¹ u, carried to the parent frame, run in
+// double-float from the FP32 velocities and the FP32 model.  In FP32 their
+// rounding (≈ 6e-8 of the body forces, summed along the tree) reaches q̈
+// through u = τ − Sᵀ p^A, where much of p^A cancels: on 2–48-DOF chains it
+// moved q̈ of 0.3 % of the instances by more than 1e-5 of |q̈| (up to 3e-5);
+// in double-float the largest error is about 2e-6.  The velocities, the bias
+// accelerations c and the product I^a c stay FP32 (they move q̈ by ≤ 1e-6).
+struct SVF {
+  FF w[3], v[3];
+};
+template <typename R>
+__device__ __forceinline__ SVF load_svf(const LaneCtx<R>& c, int base) {
+  SVF s;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    s.w[k] = ffw(c, base + k);
+    s.v[k] = ffw(c, base + 3 + k);
+  }
+  return s;
+}
+template <typename R>
+__device__ __forceinline__ void store_svf(const LaneCtx<R>& c, int base, const SVF& s) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    ffw(c, base + k) = s.w[k];
+    ffw(c, base + 3 + k) = s.v[k];
+  }
+}
+__device__ __forceinline__ SVF svf_add(const SVF& a, const SVF& b) {
+  SVF s;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    s.w[k] = ff_add(a.w[k], b.w[k]);
+    s.v[k] = ff_add(a.v[k], b.v[k]);
+  }
+  return s;
+}
+__device__ __forceinline__ SVF svf_zero() {
+  SVF s;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) s.w[k] = s.v[k] = ff(0.0f);
+  return s;
+}
+__device__ __forceinline__ SVF svf_from_double(const SV<double>& d) {
+  return {{ff_from_double(d.w.x), ff_from_double(d.w.y), ff_from_double(d.w.z)},
+          {ff_from_double(d.v.x), ff_from_double(d.v.y), ff_from_double(d.v.z)}};
+}
+
+// p = v ×* I v for the FP32 body velocity (w, vl) and the FP32 inertia (J about
+// the origin in the order xx yy zz xy xz yz, cross part cm = m·com, mass m),
+// written as p_w = w × (J w) + cm × (w × vl), p_v = m (w × vl) − w × (cm × w):
+// the same vector as (w × f_w + vl × f_v, w × f_v) with f = I v, with every
+// product of two FP32 inputs exact.
+__device__ __forceinline__ SVF bias_force_ff(const float* J, V3<float> cm, float m, V3<float> w, V3<float> vl,
+                                             bool diag) {
+  const FF g[3] = {ff_det2(w.y, vl.z, w.z, vl.y), ff_det2(w.z, vl.x, w.x, vl.z), ff_det2(w.x, vl.y, w.y, vl.x)};
+  FF h[3];  // J w
+  if (diag) {
+    h[0] = two_prod(J[0], w.x);
+    h[1] = two_prod(J[1], w.y);
+    h[2] = two_prod(J[2], w.z);
+  } else {
+    h[0] = ff_add_prod(J[4], w.z, ff_add_prod(J[3], w.y, two_prod(J[0], w.x)));
+    h[1] = ff_add_prod(J[5], w.z, ff_add_prod(J[1], w.y, two_prod(J[3], w.x)));
+    h[2] = ff_add_prod(J[2], w.z, ff_add_prod(J[5], w.y, two_prod(J[4], w.x)));
+  }
+  const FF k[3] = {ff_det2(cm.y, w.z, cm.z, w.y), ff_det2(cm.z, w.x, cm.x, w.z),
+                   ff_det2(cm.x, w.y, cm.y, w.x)};  // cm × w
+  SVF p;
+  p.w[0] = ff_add(ff_lin2(h[2], w.y, h[1], -w.z), ff_lin2(g[2], cm.y, g[1], -cm.z));
+  p.w[1] = ff_add(ff_lin2(h[0], w.z, h[2], -w.x), ff_lin2(g[0], cm.z, g[2], -cm.x));
+  p.w[2] = ff_add(ff_lin2(h[1], w.x, h[0], -w.y), ff_lin2(g[1], cm.x, g[0], -cm.y));
+  p.v[0] = ff_fmaf(k[1], w.z, ff_lin2(g[0], m, k[2], -w.y));
+  p.v[1] = ff_fmaf(k[2], w.x, ff_lin2(g[1], m, k[0], -w.z));
+  p.v[2] = ff_fmaf(k[0], w.y, ff_lin2(g[2], m, k[1], -w.x));
+  return p;
+}
+
+// A spatial force in the child frame → the parent frame, (Rr n + t × Rr f, Rr f),
+// in double-float with the FP32 transform: a rotation about principal axis
+// `planar` ≥ 0 by (co, si) turns one pair of components, otherwise Rr.
+__device__ __forceinline__ SVF force_to_parent_ff(const M3<float>& Rr, V3<float> t, const SVF& f, int planar,
+                                                  float co, float si) {
+  FF fw[3], fv[3];
+  if (planar >= 0) {
+    const int k = planar;
+    FF x, y;
+    rot2(pick3(k, f.w[1], f.w[2], f.w[0]), pick3(k, f.w[2], f.w[0], f.w[1]), co, si, x, y);
+    fw[0] = pick3(k, f.w[0], y, x);
+    fw[1] = pick3(k, x, f.w[1], y);
+    fw[2] = pick3(k, y, x, f.w[2]);
+    rot2(pick3(k, f.v[1], f.v[2], f.v[0]), pick3(k, f.v[2], f.v[0], f.v[1]), co, si, x, y);
+    fv[0] = pick3(k, f.v[0], y, x);
+    fv[1] = pick3(k, x, f.v[1], y);
+    fv[2] = pick3(k, y, x, f.v[2]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      fw[i] = ff_dot3f(f.w[0], f.w[1], f.w[2], Rr.a[3 * i], Rr.a[3 * i + 1], Rr.a[3 * i + 2]);
+      fv[i] = ff_dot3f(f.v[0], f.v[1], f.v[2], Rr.a[3 * i], Rr.a[3 * i + 1], Rr.a[3 * i + 2]);
+    }
+  }
+  SVF o;
+  o.w[0] = ff_add(fw[0], ff_lin2(fv[2], t.y, fv[1], -t.z));
+  o.w[1] = ff_add(fw[1], ff_lin2(fv[0], t.z, fv[2], -t.x));
+  o.w[2] = ff_add(fw[2], ff_lin2(fv[1], t.x, fv[0], -t.y));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) o.v[k] = fv[k];
+  return o;
+}
+
+// Bias acceleration c = v ×m (S q̇) of a body from its velocity (w, vl) (which
+// includes S q̇) and its joint velocity, as in the outward pass.
+template <typename R>
+__device__ __forceinline__ SV<R> bias_acc(int type, V3<R> ax, Col<double> v, int vo, V3<R> w, V3<R> vl) {
+  const V3<R> zero{R(0), R(0), R(0)};
+  V3<R> jw = zero, jv = zero;
+  if (type == 1) {
+    jw = ax * R(v[vo]);
+  } else if (type == 2) {
+    jv = ax * R(v[vo]);
+  } else if (type == 3) {
+    jw = {R(v[vo]), R(v[vo + 1]), R(v[vo + 2])};
+    jv = {R(v[vo + 3]), R(v[vo + 4]), R(v[vo + 5])};
+  }
+  return {cross(w, jw), cross(w, jv) + cross(vl, jw)};
+}
+
 // 6×6 Cholesky of a spatial inertia (packed lower triangle L[21], reciprocal
 // diagonal) and the solve L Lᵀ x = b.  Returns false for a non-positive pivot.
 __device__ __forceinline__ int l6(int i, int j) { return (i * (i + 1) >> 1) + j; }
@@ -584,11 +714,12 @@ template <typename R>
 __device__ __forceinline__ SV<R> sv_r(const SV<double>& s) {
   return {{R(s.w.x), R(s.w.y), R(s.w.z)}, {R(s.v.x), R(s.v.y), R(s.v.z)}};
 }
-// Row of the FP64 bias forces of a contact mechanism: F itself in the FP64
-// form; in the mixed form the separate region FD, since F holds the FP32 bias
-// forces of the pack's lanes without contacts and an FP32 row fills the first
-// half of the bytes of the FP64 row of the same index (the FP64 elements of
-// lanes 0-15).
+// Row of a contact mechanism's FP64 bias-force record: in the FP64 form region
+// F, its bias force p − f_contact; in the mixed form region FD, only the
+// contact term −f_contact (FP64), since F holds the mixed form's double-float
+// branch accumulators (and, whatever a lane writes there, every lane of the
+// pack must use the same element width: an FP32 row fills the first half of
+// the bytes of the FP64 row of the same index, the elements of lanes 0-15).
 template <typename R>
 __device__ __forceinline__ int fd_row(const LaneCtx<R>& c) {
   return sizeof(R) == 8 ? c.L.F : c.L.FD;
@@ -609,43 +740,51 @@ __device__ __forceinline__ void store_svd(const LaneCtx<R>& c, int base, const S
 
 // Pass 2 of the mixed form: articulated inertias, U, D and the congruence to
 // the parent in double-float, from the FP32 model and the FP32 transforms of
-// pass 1; bias forces in FP32 (FP64 for contact mechanisms, as in the FP64
-// form).  A 1-DOF joint's DU record holds FF words (U, 1/D, u); a floating
-// joint's holds the FP64 record of the FP64 form.
+// pass 1; each body's bias force p = v ×* I v (from its FP32 velocity, plus
+// the FP64 contact wrench of a contact mechanism) and the bias-force
+// recursion in double-float; the bias acceleration c and I^a c in FP32.  A
+// 1-DOF joint's DU record holds FF words (U, 1/D, u); a floating joint's holds
+// the FP64 record of the FP64 form.
 template <typename R>
-__device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q, Col<double> tau, bool have_tau,
-                                             bool contacts) {
+__device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<double> tau,
+                                             bool have_tau, bool contacts) {
   using V = V3<R>;
-  using VD = V3<double>;
   int st = 0;
   ABIF carryI;
-  SV<R> carryP;
+  SVF carryP;
   int ctarget = -1;
   for (int b = c.nb - 1; b >= 0; --b) {
     const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
     const uint32_t fl = w1 & 255;
     const int type = w0 & 15, parent = (w0 >> 4) & 255, qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
     const int tb = TOPO_D * b;
-    ABIF IA = body_abi_ff(c, tb);
-    SV<double> pAd;
-    SV<R> pA;
-    if (contacts) {
-      pAd = load_svd(c, fd_row(c) + 6 * b);
-      if (ctarget == b) pAd = pAd + sv_d(carryP);
-      pA = sv_r<R>(pAd);
-    } else {
-      pA = load_sv(c, c.L.F + 6 * b);
-      if (ctarget == b) pA = pA + carryP;
+    const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
+    // bias terms from the body velocity of pass 1
+    const SV<R> vb = load_sv(c, c.L.V + 6 * b);
+    const SV<R> cb = bias_acc(type, ax, v, vo, vb.w, vb.v);
+    SVF pA;
+    {
+      float J[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) J[k] = c.t(tb + TD_INERTIA + 4 + k);
+      const V cm{c.t(tb + TD_INERTIA + 1), c.t(tb + TD_INERTIA + 2), c.t(tb + TD_INERTIA + 3)};
+      pA = bias_force_ff(J, cm, c.t(tb + TD_INERTIA), vb.w, vb.v, (fl & BF_DIAG_INERTIA) != 0);
     }
-    if (fl & BF_BRANCH) abi_add(IA, load_abi_ff(c, c.L.AI + ABI_D * b));
-    if (ctarget == b) abi_add(IA, carryI);
-    const SV<R> cb = load_sv(c, c.L.A + 6 * b);
-    SV<R> pa;
+    if (contacts) pA = svf_add(pA, svf_from_double(load_svd(c, fd_row(c) + 6 * b)));  // − contact wrench
+    ABIF IA = body_abi_ff(c, tb);
+    if (fl & BF_BRANCH) {
+      abi_add(IA, load_abi_ff(c, c.L.AI + ABI_D * b));
+      pA = svf_add(pA, load_svf(c, c.L.F + 6 * b));
+    }
+    if (ctarget == b) {
+      abi_add(IA, carryI);
+      pA = svf_add(pA, carryP);
+    }
+    SVF pa;
     const bool to_parent = parent != 0;
     const int planar = planar_axis(type, fl);
     if (type == 1 || type == 2) {
       FF Uw[3], Uv[3], D;
-      const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
       if (type == 1 && (fl & BF_AXIS_PRINCIPAL)) {  // a = ±e_k: U = ±(A[:,k], row k of B), D = A_kk
         const int k = (int)bf_axis_index(fl);
         Uw[0] = pick3(k, IA.A[0], IA.A[3], IA.A[4]);
@@ -676,16 +815,13 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
         }
         D = ff_dot3f(Uv[0], Uv[1], Uv[2], ax.x, ax.y, ax.z);
       }
-      // u = τ + τ_spring − Sᵀ p^A (FP64, as in the FP64 form, then split)
-      double u = have_tau ? tau[vo] : 0.0;
+      // u = τ + τ_spring − Sᵀ p^A (the torque in FP64, split; Sᵀ p^A in double-float)
+      double tt = have_tau ? tau[vo] : 0.0;
       if (type == 2 && (w1 & BF_SPRING) && c.springs)
-        u += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
-      if (contacts) {
-        const VD axd{c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
-        u -= type == 1 ? dot(axd, pAd.w) : dot(axd, pAd.v);
-      } else {
-        u -= double(type == 1 ? dot(ax, pA.w) : dot(ax, pA.v));
-      }
+        tt += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
+      const FF sp = type == 1 ? ff_dot3f(pA.w[0], pA.w[1], pA.w[2], ax.x, ax.y, ax.z)
+                              : ff_dot3f(pA.v[0], pA.v[1], pA.v[2], ax.x, ax.y, ax.z);
+      const FF uf = ff_sub(ff_from_double(tt), sp);
       if (type == 1) {  // revolute armature (src/hybrid/articulated/mod.rs:244-247)
         const float arm = c.t(tb + TD_ARMATURE);
         if (arm != 0.0f) D = ff_add(D, ff(arm));
@@ -693,7 +829,6 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
       D = two_sum(D.hi, D.lo);  // ff_rcp starts from D.hi
       if (!(D.hi > 0.0f)) st |= 2;  // GPB_ST_CHOL_FAIL
       const FF Dinv = ff_rcp(D);
-      const FF uf = ff_from_double(u);
       const int du = c.L.DU + DU_D * vo;
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
@@ -703,7 +838,7 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
       ffw(c, du + 6) = Dinv;
       ffw(c, du + 7) = uf;
       if (to_parent) {
-        // I^a = I^A − U D⁻¹ Uᵀ ; p^a = p^A + I^a c + U D⁻¹ u (FP32)
+        // I^a = I^A − U D⁻¹ Uᵀ ; p^a = p^A + I^a c + U D⁻¹ u
         FF Ww[3], Wv[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
@@ -720,9 +855,14 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int j = 0; j < 3; ++j) IA.B[3 * i + j] = ff_fms(IA.B[3 * i + j], Ww[i], Uv[j]);
-        const R ud = ff_f(ff_mul(uf, Dinv));
-        const SV<R> Ur{{ff_f(Uw[0]), ff_f(Uw[1]), ff_f(Uw[2])}, {ff_f(Uv[0]), ff_f(Uv[1]), ff_f(Uv[2])}};
-        pa = pA + abi_mul_hi(IA, cb) + scale(Ur, ud);
+        const FF ud = ff_mul(uf, Dinv);
+        const SV<R> iac = abi_mul_hi(IA, cb);
+        const R iw[3] = {iac.w.x, iac.w.y, iac.w.z}, iv[3] = {iac.v.x, iac.v.y, iac.v.z};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          pa.w[i] = ff_add(pA.w[i], ff_fma(Uw[i], ud, ff(iw[i])));
+          pa.v[i] = ff_add(pA.v[i], ff_fma(Uv[i], ud, ff(iv[i])));
+        }
       }
     } else if (type == 3) {  // floating joint: the FP64 6×6 solve of the FP64 form
       double L[21], dinv[6];
@@ -732,27 +872,33 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
       for (int k = 0; k < 21; ++k) c.d(du + k) = L[k];
 #pragma unroll
       for (int k = 0; k < 6; ++k) c.d(du + 21 + k) = dinv[k];
-      const SV<double> pp = contacts ? pAd : sv_d(pA);
-      const double pv6[6] = {pp.w.x, pp.w.y, pp.w.z, pp.v.x, pp.v.y, pp.v.z};
-      R pa6[6];
+      const FF p6[6] = {pA.w[0], pA.w[1], pA.w[2], pA.v[0], pA.v[1], pA.v[2]};
+      FF pa6[6];
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
-        const double u = (have_tau ? tau[vo + k] : 0.0) - pv6[k];
+        const double pv = ff_to_double(p6[k]);
+        const double u = (have_tau ? tau[vo + k] : 0.0) - pv;
         c.d(du + 27 + k) = u;
-        pa6[k] = R(double(pv6[k]) + u);  // floating joint: I^a = 0, p^a = p^A + u
+        pa6[k] = ff_from_double(pv + u);  // floating joint: I^a = 0, p^a = p^A + u
       }
       pa = {{pa6[0], pa6[1], pa6[2]}, {pa6[3], pa6[4], pa6[5]}};
     } else {  // fixed joint: I^a = I^A, p^a = p^A + I^A c
-      pa = pA + abi_mul_hi(IA, cb);
+      const SV<R> iac = abi_mul_hi(IA, cb);
+      const R iw[3] = {iac.w.x, iac.w.y, iac.w.z}, iv[3] = {iac.v.x, iac.v.y, iac.v.z};
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        pa.w[i] = ff_addf(pA.w[i], iw[i]);
+        pa.v[i] = ff_addf(pA.v[i], iv[i]);
+      }
     }
     if (to_parent) {
       const int pb = parent - 1;
       M3<R> RrR;
       V tr;
       load_xf(c, b, planar, RrR, tr);
+      const R co = planar >= 0 ? c.r(c.L.RF + 12 * b) : R(1);
+      const R si = planar >= 0 ? c.r(c.L.RF + 12 * b + 1) : R(0);
       if (type != 3) {
-        const R co = planar >= 0 ? c.r(c.L.RF + 12 * b) : R(1);
-        const R si = planar >= 0 ? c.r(c.L.RF + 12 * b + 1) : R(0);
         const ABIF Ip = abi_to_parent(IA, RrR, tr, planar, co, si);
         if (pb == b - 1) {
           carryI = Ip;
@@ -764,14 +910,12 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
       } else if (pb == b - 1) {
         carryI = ABIF{};  // floating joint below the parent: I^a = 0
       }
-      // force to the parent frame: (Rr n + t × Rr f, Rr f)
-      const SV<R> fp = force_to_parent(RrR, tr, pa);
+      const SVF fp = force_to_parent_ff(RrR, tr, pa, planar, co, si);
       if (pb == b - 1) {
         carryP = fp;
         ctarget = pb;
       } else {
-        if (contacts) store_svd(c, fd_row(c) + 6 * pb, load_svd(c, fd_row(c) + 6 * pb) + sv_d(fp));
-        else store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
+        store_svf(c, c.L.F + 6 * pb, svf_add(load_svf(c, c.L.F + 6 * pb), fp));
         ctarget = -1;
       }
     } else {
@@ -946,15 +1090,19 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       om = om + jw;
       vl = vl + jv;
     }
-    const SV<R> cb{cross(om, jw), cross(om, jv) + cross(vl, jw)};
-    // bias force p = v ×* I v − f_contact (body frame)
-    SI<R> I;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) I.j[k] = c.t(tb + TD_INERTIA + 4 + k);
-    I.c = {c.t(tb + TD_INERTIA + 1), c.t(tb + TD_INERTIA + 2), c.t(tb + TD_INERTIA + 3)};
-    I.m = c.t(tb + TD_INERTIA);
     const SV<R> vb{om, vl};
-    SV<R> p = crf(vb, imul(I, vb));
+    // bias acceleration c and bias force p = v ×* I v − f_contact (body frame);
+    // the mixed form forms both in pass 2 from the stored velocity
+    SV<R> cb, p;
+    if constexpr (sizeof(R) == 8) {
+      cb = {cross(om, jw), cross(om, jv) + cross(vl, jw)};
+      SI<R> I;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) I.j[k] = c.t(tb + TD_INERTIA + 4 + k);
+      I.c = {c.t(tb + TD_INERTIA + 1), c.t(tb + TD_INERTIA + 2), c.t(tb + TD_INERTIA + 3)};
+      I.m = c.t(tb + TD_INERTIA);
+      p = crf(vb, imul(I, vb));
+    }
     // contact wrench (body frame), FP64: stiff contacts make it the largest term
     // of the bias force, and the root's u = τ − p^A reads it directly
     SV<double> wc{{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
@@ -1063,14 +1211,23 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       c.r(c.L.RF + 12 * b + 10) = t.y;
       c.r(c.L.RF + 12 * b + 11) = t.z;
     }
-    store_sv(c, c.L.A + 6 * b, cb);
-    if (contacts) store_svd(c, fd_row(c) + 6 * b, sv_d(p) + wc);  // bias forces of contact mechanisms: FP64
-    else store_sv(c, c.L.F + 6 * b, p);
+    if constexpr (sizeof(R) == 8) {
+      store_sv(c, c.L.A + 6 * b, cb);
+      if (contacts) store_svd(c, fd_row(c) + 6 * b, sv_d(p) + wc);  // bias forces of contact mechanisms: FP64
+      else store_sv(c, c.L.F + 6 * b, p);
+    } else {
+      store_sv(c, c.L.V + 6 * b, vb);  // passes 2 and 3 form c and p from it
+      if (contacts) store_svd(c, fd_row(c) + 6 * b, wc);
+    }
     if (fl & BF_BRANCH) {
-      // accumulator for children other than b+1
-      if (sizeof(R) == 8) store_abi(c, c.L.AI + ABI_D * b, ABI{});
-      else store_abi_ff(c, c.L.AI + ABI_D * b, ABIF{});
-      store_sv(c, c.L.V + 6 * b, vb);
+      // accumulators for children other than b+1
+      if (sizeof(R) == 8) {
+        store_abi(c, c.L.AI + ABI_D * b, ABI{});
+        store_sv(c, c.L.V + 6 * b, vb);
+      } else {
+        store_abi_ff(c, c.L.AI + ABI_D * b, ABIF{});
+        store_svf(c, c.L.F + 6 * b, svf_zero());
+      }
       if (dvel) store_svd(c, c.L.VW + 6 * b, SV<double>{omd, vld});
       if (contacts) {
 #pragma unroll
@@ -1099,7 +1256,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
   // A child that is the next body (every link of a chain) hands its terms to
   // the parent in registers; other children accumulate into the parent's slot.
   if constexpr (sizeof(R) == 4) {
-    st |= aba_inward_ff(c, q, tau, have_tau, contacts);
+    st |= aba_inward_ff(c, q, v, tau, have_tau, contacts);
   } else {
     ABI carryI;
     SV<R> carryP;
@@ -1287,10 +1444,19 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     M3<R> Rr;
     V t;
     load_xf(c, b, planar_axis(type, w1 & 255), Rr, t);
-    // a' = X a_p + c
+    const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
+    // a' = X a_p + c (the mixed form forms c again from the body velocity,
+    // which a branch body's acceleration overwrites only below)
+    SV<R> cb;
+    if constexpr (sizeof(R) == 8) {
+      cb = load_sv(c, c.L.A + 6 * b);
+    } else {
+      const SV<R> vb = load_sv(c, c.L.V + 6 * b);
+      cb = bias_acc(type, ax, v, vo, vb.w, vb.v);
+    }
     a.v = mulT(Rr, a.v + cross(a.w, t));
     a.w = mulT(Rr, a.w);
-    a = a + load_sv(c, c.L.A + 6 * b);
+    a = a + cb;
     const int du = c.L.DU + DU_D * vo;
     if (type == 1 || type == 2) {
       double x;
@@ -1315,7 +1481,6 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       }
       qdd[vo] = x;
       if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
-      const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
       if (type == 1) a.w = a.w + ax * xr;
       else a.v = a.v + ax * xr;
     } else if (type == 3) {

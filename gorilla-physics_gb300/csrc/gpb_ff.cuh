@@ -100,6 +100,34 @@ __device__ __forceinline__ FF ff_dot3f(FF a0, FF a1, FF a2, float x0, float x1, 
   return ff_fmaf(a2, x2, ff_lin2(a0, x0, a1, x1));
 }
 
+// Exact products of FP32 operands.
+__device__ __forceinline__ FF two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+// a·b − c·d for FP32 operands (a cross-product component): both products
+// exact, their difference one exact sum of the leading terms.
+__device__ __forceinline__ FF ff_det2(float a, float b, float c, float d) {
+  const float p = __fmul_rn(a, b);
+  const float e1 = __fmaf_rn(a, b, -p);
+  const float r = __fmul_rn(c, d);
+  const float e2 = __fmaf_rn(c, d, -r);
+  const FF s = two_sum(p, -r);
+  return {s.hi, __fadd_rn(s.lo, __fsub_rn(e1, e2))};
+}
+// c + a·b for FP32 a, b (the product exact).
+__device__ __forceinline__ FF ff_add_prod(float a, float b, FF c) {
+  const float p = __fmul_rn(a, b);
+  const float e = __fmaf_rn(a, b, -p);
+  const FF s = two_sum(p, c.hi);
+  return {s.hi, __fadd_rn(s.lo, __fadd_rn(e, c.lo))};
+}
+// a + f for an FP32 f.
+__device__ __forceinline__ FF ff_addf(FF a, float f) {
+  const FF s = two_sum(a.hi, f);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+
 // 1/d: the FP32 reciprocal refined by one Newton step, r + r·(1 − d·r), with
 // the residual formed exactly from the FF product.
 __device__ __forceinline__ FF ff_rcp(FF d) {

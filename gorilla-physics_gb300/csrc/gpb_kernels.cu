@@ -1127,7 +1127,12 @@ struct EvalOf<2> {
 // velocity recursion of contact mechanisms, which costs the chains
 // (lane-per-instance code without contacts) their spare occupancy.
 template <int PREC>
-__global__ void __launch_bounds__(128, PREC == 1 ? 3 : 1) simulate_kernel(DeviceBatch b, StepParams p) {
+// Resident 4-warp blocks per SM the mixed form's step kernel is compiled for
+// (its register budget: 3 blocks = 168 registers a thread, 2 blocks = 255).
+#ifndef GPB_MIXED_MIN_BLOCKS
+#define GPB_MIXED_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(128, PREC == 1 ? GPB_MIXED_MIN_BLOCKS : 1) simulate_kernel(DeviceBatch b, StepParams p) {
   const int lane = threadIdx.x & 31;
   // packs [0, ncoop): one whole block per pack (large mechanisms, largest first)
   if (PREC != 2 && p.ncoop > 0) {

@@ -106,5 +106,5 @@ def test_armature_in_refined_and_mixed_forms(ctx):
     ex = np.array([rel(x[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]) for i in range(M.n)])
     ef = [rel(f[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]) for i in range(M.n)]
     assert max(er) < 1e-7 and max(ef) < 1e-8
-    assert np.mean(ex <= 1e-5) >= 0.99
+    assert ex.max() <= 1e-5, ex.max()
     B.close()

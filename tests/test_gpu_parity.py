@@ -115,12 +115,12 @@ def test_config_dynamics_fp64(ctx, config, n, model):
     assert np.all(B.status() == 0)
 
 
-@pytest.mark.parametrize("config,n,model", [(0, 256, 1), (1, 1024, 1), (2, 256, 1), (2, 256, 0),
-                                            (3, 128, 1), (3, 128, 0)])
+@pytest.mark.parametrize("config,n,model", [(0, 1024, 1), (1, 16384, 1), (2, 4096, 1), (2, 4096, 0),
+                                            (3, 2048, 1), (3, 2048, 0)])
 def test_mixed_aba_error_bound(ctx, algorithm, config, n, model):
     """MIXED with the articulated-body algorithm (double-float articulated
-    inertias, FP32 kinematics): q̈ within 1e-5 of FP64 (relative to
-    max(|q̈|, 1)) on at least 99 % of instances, and within 1e-4 on all of them."""
+    inertias and bias forces, FP32 kinematics): every instance's q̈ within 1e-5
+    of FP64 (relative to max(|q̈|, 1))."""
     if algorithm != "aba":
         pytest.skip("the bound is a property of the ABA form of MIXED")
     M, q0, v0, _ = Model.from_config(config, n, seed=13, contact_model=model)
@@ -136,8 +136,7 @@ def test_mixed_aba_error_bound(ctx, algorithm, config, n, model):
     a = B.dynamics_continuous(tau, precision=gpb.FP64)
     b = B.dynamics_continuous(tau, precision=gpb.MIXED)
     errs = np.array([rel_err(b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]) for i in range(M.n)])
-    assert np.mean(errs <= 1e-5) >= 0.99, (np.mean(errs <= 1e-5), np.quantile(errs, 0.99))
-    assert errs.max() <= 1e-4, errs.max()
+    assert errs.max() <= 1e-5, (errs.max(), int(np.argmax(errs)))
 
 
 def _pack_kinds(M):
@@ -156,7 +155,7 @@ def test_mixed_contact_batches(ctx, algorithm, precision):
     """Quadrupeds (contacts) batched with serial chains (none), so that packs
     hold both kinds: every instance's q̈ is bit-identical to the one it gets in
     a batch of its own kind (a lane reads and writes nothing of its
-    neighbours), MIXED with the articulated-body algorithm stays within 1e-4 of
+    neighbours), MIXED with the articulated-body algorithm stays within 1e-5 of
     FP64 (relative to max(|q̈|, 1)), MIXED_REFINED within 1e-6, and no status
     bit is set.  A mixed pack once let the FP32 bias forces of its
     chain lanes overwrite the FP64 bias forces of its contact lanes."""
@@ -186,7 +185,7 @@ def test_mixed_contact_batches(ctx, algorithm, precision):
         np.testing.assert_array_equal(mix[sl], alone)
         A.close()
     # MIXED with CRBA is the FP32 mass-matrix form, limited by cond(H)·ε32: no bound
-    bound = {gpb.FP64: 0.0, gpb.MIXED: 1e-4 if algorithm == "aba" else None, gpb.MIXED_REFINED: 1e-6}[precision]
+    bound = {gpb.FP64: 0.0, gpb.MIXED: 1e-5 if algorithm == "aba" else None, gpb.MIXED_REFINED: 1e-6}[precision]
     if bound is not None:
         _, vo, _ = M.offsets()
         errs = np.array([rel_err(mix[vo[i]:vo[i + 1]], ref[vo[i]:vo[i + 1]]) for i in range(M.n)])
@@ -254,8 +253,7 @@ def test_general_trees(ctx, algorithm):
         return
     b = B.dynamics_continuous(tau, precision=gpb.MIXED)
     errs = np.array([rel_err(b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]) for i in range(M.n)])
-    assert np.mean(errs <= 1e-5) >= 0.99, (np.mean(errs <= 1e-5), np.quantile(errs, 0.99))
-    assert errs.max() <= 1e-4, errs.max()
+    assert errs.max() <= 1e-5, (errs.max(), int(np.argmax(errs)))
     assert np.all(B.status() == 0)
 
 
