@@ -345,13 +345,6 @@ extern "C" int gpb_batch_layout(const gpb_batch* b, int64_t* q_offset, int64_t* 
   return GPB_OK;
 }
 
-extern "C" int gpb_batch_set_mapping(gpb_batch* b, int lanes) {
-  if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_mapping: batch is NULL");
-  if (lanes != 0 && lanes != 1) return fail(GPB_E_INVAL, "gpb_batch_set_mapping: lanes must be 0 or 1");
-  b->mapping = lanes;
-  return GPB_OK;
-}
-
 extern "C" int gpb_batch_set_algorithm(gpb_batch* b, int algorithm) {
   if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_algorithm: batch is NULL");
   if (algorithm != GPB_ALGO_CRBA && algorithm != GPB_ALGO_ABA)
@@ -556,7 +549,7 @@ static int run_simulate(gpb_batch* b, double dt, int64_t K, int64_t step0, int i
   p.ncoop = coop_packs(b, precision);
   if (b->npacks > 0 && K > 0) {
     CUDA_TRY(cudaEventRecord(b->ctx->ev0, s));
-    CUDA_TRY(launch_simulate(b->dev(), p, b->mapping, b->ctx->num_sms, b->warps_per_sm, s));
+    CUDA_TRY(launch_simulate(b->dev(), p, b->ctx->num_sms, b->warps_per_sm, s));
     CUDA_TRY(cudaEventRecord(b->ctx->ev1, s));
     b->ctx->timed = true;
     b->ctx->launches++;

@@ -205,7 +205,6 @@ struct gpb_batch {
   gpb_ctx* ctx = nullptr;
   int64_t n = 0;
   int32_t npacks = 0;
-  int mapping = 0;
   int warps_per_sm = 0;  // resident warps per SM of the step kernel (0 = occupancy limit)
   int coop_min_dof = -1; // block-cooperative packs: DOF threshold (-1 = default, 0 = off)
   int algorithm = GPB_ALGO_CRBA;

@@ -235,7 +235,7 @@ struct StepParams {
 // Launchers (gpb_kernels.cu).  All return a cudaError_t.
 // warps_per_sm: resident warps per SM of the persistent grid (0 = the
 // occupancy limit; otherwise rounded to whole 4-warp blocks and capped by it).
-cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes_per_instance,
+cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p,
                             int num_sms, int warps_per_sm, cudaStream_t s);
 cudaError_t launch_dynamics(const DeviceBatch& b, const StepParams& p, cudaStream_t s);
 // Resident warps per SM the step kernel of `precision` can hold (registers).

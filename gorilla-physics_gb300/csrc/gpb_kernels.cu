@@ -1343,9 +1343,8 @@ cudaError_t launch_collide(int64_t n, const double* pose_a, const double* size_a
   return cudaGetLastError();
 }
 
-cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int lanes_per_instance,
-                            int num_sms, int warps_per_sm, cudaStream_t s) {
-  (void)lanes_per_instance;
+cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int num_sms, int warps_per_sm,
+                            cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(b.queue, 0, 2 * sizeof(int32_t), s);
   if (e != cudaSuccess) return e;
   const int threads = 128;

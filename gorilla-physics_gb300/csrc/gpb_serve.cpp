@@ -604,7 +604,7 @@ extern "C" int gpb_server_tick(gpb_server* S, int32_t* completed_now) {
   p.precision = S->opts.precision;
   p.dt = 1.0;  // per-slot values come from the jobs
   CUDA_TRY(cudaEventRecord(S->ctx->ev0, s));
-  CUDA_TRY(launch_simulate(db, p, 1, S->ctx->num_sms, 0, s));
+  CUDA_TRY(launch_simulate(db, p, S->ctx->num_sms, 0, s));
   CUDA_TRY(cudaEventRecord(S->ctx->ev1, s));
   S->ctx->timed = true;
   S->ctx->launches++;

@@ -127,7 +127,6 @@ SIGNATURES = [
     ("gpb_batch_clear_status", C.c_int, [C.c_void_p]),
     ("gpb_batch_steps_done", C.c_int, [C.c_void_p, P_i64]),
     ("gpb_synchronize", C.c_int, [C.c_void_p]),
-    ("gpb_batch_set_mapping", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_batch_set_launch", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_batch_set_coop", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_batch_set_algorithm", C.c_int, [C.c_void_p, C.c_int]),

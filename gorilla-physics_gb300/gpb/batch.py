@@ -152,10 +152,6 @@ class Batch:
     def clear_status(self) -> None:
         _abi.check(_abi.lib().gpb_batch_clear_status(self.h), "gpb_batch_clear_status")
 
-    def set_mapping(self, lanes_per_instance: int) -> None:
-        _abi.check(_abi.lib().gpb_batch_set_mapping(self.h, lanes_per_instance),
-                   "gpb_batch_set_mapping")
-
     def set_gravity(self, g: float) -> None:
         """Gravitational acceleration along −z (default 9.81; 0 = off)."""
         _abi.check(_abi.lib().gpb_batch_set_gravity(self.h, g), "gpb_batch_set_gravity")

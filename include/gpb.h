@@ -104,10 +104,12 @@ enum gpb_precision { GPB_FP64 = 0, GPB_MIXED = 1, GPB_MIXED_REFINED = 2 };
  * GPB_ALGO_ABA: Featherstone's articulated-body algorithm in link coordinates,
  *   O(n) per instance; the same q̈ in exact arithmetic (FP64 results agree with
  *   CRBA to the conditioning bound).  With GPB_MIXED its articulated-inertia
- *   recursion and the 1-DOF q̈ solve run in double-float (pairs of FP32
- *   numbers, about 48 bits, on the FP32 pipes) from the FP32-rounded model,
- *   kinematics and bias forces in FP32, the state, u = τ − Sᵀp^A and a
- *   floating root's 6×6 solve in FP64.  GPB_MIXED_REFINED always uses CRBA. */
+ *   recursion, the body bias forces v ×* I v with their inward recursion and
+ *   the 1-DOF q̈ solve run in double-float (pairs of FP32 numbers, about 48
+ *   bits, on the FP32 pipes) from the FP32-rounded model; kinematics,
+ *   velocities and bias accelerations in FP32; the state, contact wrenches of
+ *   contact mechanisms and a floating root's 6×6 solve in FP64.
+ *   GPB_MIXED_REFINED always uses CRBA. */
 enum gpb_algorithm { GPB_ALGO_CRBA = 0, GPB_ALGO_ABA = 1 };
 
 /* GPB_HUNT_CROSSLEY: src/contact.rs:260-338 (k = k_p k_h/(k_p+k_h), k_h = 50e3,
@@ -339,11 +341,8 @@ int gpb_batch_steps_done(gpb_batch* batch, int64_t* steps);
 int gpb_synchronize(gpb_ctx* ctx);
 
 /* ---- kernel mapping ---------------------------------------------------- */
-/*
- * Lanes cooperating on one instance: 1 (32 instances per warp, serial sweeps),
- * or 0 = let the library choose per size class (the autotuned default).
- */
-int gpb_batch_set_mapping(gpb_batch* batch, int lanes_per_instance);
+/* One lane steps one instance (a warp steps a pack of 32), or, for the CRBA
+ * route, the four warps of a block share one pack (gpb_batch_set_coop). */
 
 /* Resident warps per SM of the persistent step kernel (one warp per pack of
  * 32 instances): 0 = as many as the kernel's registers allow (the default),

@@ -148,6 +148,19 @@ def cart_pole(mc=3.0, lc=1.0, mp=5.0, lp=7.0, axis_pole=(0, 1, 0)):
     return MechanismState(j, b)
 
 
+def spring_pair(m=1.0, r=0.1, k=50.0, l_rest=2.0 / 3.0):
+    """spring_on_frictionless_ground (src/dynamics.rs:1133-1188): two spheres,
+    A on a floating joint, B on a prismatic joint along A's x axis with a
+    spring (k, l_rest); their sphere colliders take no part in the continuous
+    dynamics, so the ground half-space exerts nothing."""
+    mom = 2.0 / 5.0 * m * r * r
+    s = MechanismState([FloatingJoint(Transform3D("A", WORLD_FRAME)),
+                        PrismaticJoint(Transform3D("B", "A"), (1.0, 0.0, 0.0), spring=(k, l_rest))],
+                       [body("A", m, (mom, mom, mom), (0, 0, 0)), body("B", m, (mom, mom, mom), (0, 0, 0))])
+    s.add_halfspace(HalfSpace.new((0, 0, 1), 0.0, 1.0, 0.0))
+    return s
+
+
 def sphere_point(m=1.0, r=0.1):
     """mass_hit_ground (src/contact.rs:607-675): floating sphere + centre contact."""
     mom = 2.0 / 5.0 * m * r * r

@@ -257,6 +257,77 @@ def test_general_trees(ctx, algorithm):
     assert np.all(B.status() == 0)
 
 
+def test_spring_on_frictionless_ground_gpu(ctx):
+    """src/dynamics.rs:1133-1188 through the GPU (RK4, 1.1 s): a prismatic spring
+    between two free spheres keeps their midpoint at l_init/2 (1e-5); 64 copies
+    with different initial extensions, each on the oracle's trajectory (1e-9)."""
+    from tests.test_oracle_kats import spring_midpoint
+
+    n = 64
+    rng = np.random.default_rng(8)
+    l0 = np.concatenate([[2.0], rng.uniform(0.5, 3.0, n - 1)])
+    M = Model.from_mechanisms([kats.spring_pair(l_rest=2.0 / 3.0) for _ in range(n)])
+    q0 = np.concatenate([[0, 0, 0, 1, 0, 0, 0, x] for x in l0])
+    B = Batch(M, ctx)
+    B.update(q0, np.zeros(7 * n))
+    K = gpb.simulate_steps(1.1, 1e-3)
+    B.simulate_steps(K, 1e-3, gpb.RUNGE_KUTTA_4)
+    q, _ = B.state()
+    assert np.all(B.status() == 0)
+    xa, xb, mid = spring_midpoint(q[0:8])
+    assert abs(mid - 1.0) < 1e-5 and xa > 0.0 and xb < 2.0
+    for i in range(0, n, 9):
+        qr, _, st, _ = oracle.simulate(M, i, q0[8 * i:8 * i + 8], np.zeros(7), 1e-3, K, gpb.RUNGE_KUTTA_4,
+                                       oracle.CHOLESKY)
+        assert st == 0 and rel_err(q[8 * i:8 * i + 8], qr) < 1e-9, i
+        assert abs(spring_midpoint(q[8 * i:8 * i + 8])[2] - l0[i] / 2.0) < 1e-5
+
+
+def test_sprung_prismatic_trees(ctx, algorithm):
+    """Trees whose prismatic joints carry springs (src/dynamics.rs:298-315):
+    FP64 q̈ against the oracle (1e-9), MIXED (ABA) against FP64 (1e-5)."""
+    from gpb.model import (WORLD_FRAME, MechanismState, PrismaticJoint, RevoluteJoint, RigidBody,
+                           SpatialInertia, Transform3D)
+
+    rng = np.random.default_rng(12)
+    mechs = []
+    for _ in range(256):
+        joints, bodies = [], []
+        for k in range(int(rng.integers(2, 7))):
+            frame, parent = f"b{k}", WORLD_FRAME if k == 0 else f"b{int(rng.integers(0, k))}"
+            axis = rng.normal(size=3)
+            axis /= np.linalg.norm(axis)
+            tr = Transform3D(frame, parent, translation=tuple(rng.uniform(-0.5, 0.5, 3)))
+            if k == 0 or rng.uniform() < 0.6:
+                joints.append(PrismaticJoint(tr, axis, spring=(rng.uniform(5.0, 200.0), rng.uniform(-0.5, 0.5))))
+            else:
+                joints.append(RevoluteJoint(tr, axis))
+            m = rng.uniform(0.3, 2.0)
+            bodies.append(RigidBody(SpatialInertia(frame, np.diag(rng.uniform(0.01, 0.1, 3)), (0.0, 0.0, 0.0), m)))
+        mechs.append(MechanismState(joints, bodies))
+    M = Model.from_mechanisms(mechs)
+    assert np.count_nonzero(M.joint_spring[0::2]) >= 256
+    qo, vo, _ = M.offsets()
+    q0 = rng.uniform(-1.0, 1.0, qo[-1])
+    v0 = rng.normal(size=vo[-1])
+    B = Batch(M, ctx)
+    B.update(q0, v0)
+    a = B.dynamics_continuous(None, precision=gpb.FP64)
+    for i in range(M.n):
+        ref, st = oracle.dynamics(M, i, q0[qo[i]:qo[i + 1]], v0[vo[i]:vo[i + 1]])
+        assert st == 0 and rel_err(a[vo[i]:vo[i + 1]], ref) <= 1e-9, i
+    # the spring term is present: without it the oracle's q̈ differs
+    Mn = Model.from_mechanisms(mechs)
+    Mn.joint_spring[:] = 0.0
+    ref0, _ = oracle.dynamics(Mn, 0, q0[qo[0]:qo[1]], v0[vo[0]:vo[1]])
+    assert rel_err(a[vo[0]:vo[1]], ref0) > 1e-3
+    if algorithm == "aba":
+        b = B.dynamics_continuous(None, precision=gpb.MIXED)
+        errs = np.array([rel_err(b[vo[i]:vo[i + 1]], a[vo[i]:vo[i + 1]]) for i in range(M.n)])
+        assert errs.max() <= 1e-5, errs.max()
+    assert np.all(B.status() == 0)
+
+
 def test_mixed_precision_error(ctx):
     """MIXED on C1 chains: finite, and the FP32 build error is what it is
     (reported by the benchmark; not the ≤1e-5 mode)."""

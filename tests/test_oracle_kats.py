@@ -162,3 +162,27 @@ def test_ball_fall(built):
     exp = (math.pi / 2 + 5.0) % (2 * math.pi)
     exp = min(exp, 2 * math.pi - exp)
     assert abs(angle - exp) < 1e-2
+
+
+def spring_midpoint(q):
+    """x of A, x of B and their midpoint for the spring pair's q = (floating A, prismatic B)."""
+    x, y, z, w = q[0:4]
+    r00 = 1.0 - 2.0 * (y * y + z * z)  # x component of A's x axis in the world
+    xa = q[4]
+    xb = xa + r00 * q[7]
+    return xa, xb, 0.5 * (xa + xb)
+
+
+def test_spring_on_frictionless_ground(built):
+    """src/dynamics.rs:1133-1188: a prismatic spring between two free spheres,
+    RK4 for 1.1 s — the midpoint stays at l_init/2 (1e-5), A at x > 0, B at x < l_init."""
+    l_init = 2.0
+    M = Model.from_mechanisms([kats.spring_pair(l_rest=l_init / 3.0)])
+    K = gpb.simulate_steps(1.1, 1e-3)
+    q0 = np.array([0, 0, 0, 1, 0, 0, 0, l_init], float)
+    q, v, st, _ = oracle.simulate(M, 0, q0, np.zeros(7), 1e-3, K, gpb.RUNGE_KUTTA_4)
+    assert st == 0
+    xa, xb, mid = spring_midpoint(q)
+    assert abs(mid - l_init / 2.0) < 1e-5
+    assert xa > 0.0 and xb < l_init
+    assert abs(q[7] - l_init) > 0.1  # the spring did move the spheres
