@@ -421,34 +421,52 @@ __device__ __forceinline__ void shift_general(const FF* A, const FF* B, const FF
     o.C[k] = Cm[3 * i + j];
   }
 }
-// abi_to_parent in double-float: the child's FP32 transform (Rr, t), or its
-// (co, si) about principal axis `planar`.
-__device__ __forceinline__ ABIF abi_to_parent(const ABIF& I, const M3<float>& Rr, V3<float> t, int planar, float co,
-                                              float si) {
-  FF A[9], B[9], Cm[9];
-  FF a6[6], c6[6];
+// abi_to_parent in double-float, in place on packed blocks: the rotation of
+// every block (a planar rotation when `planar` ≥ 0), then the shift by t with
+// B_p = B' + T C', A_p = A' − B_p T − (B' T)ᵀ, C_p = C' (T = [t]×).  Fewer live
+// values than expanding the symmetric blocks to 3×3.
+__device__ __forceinline__ void abi_to_parent_inplace(ABIF& I, const M3<float>& Rr, V3<float> t, int planar,
+                                                      float co, float si) {
   if (planar >= 0) {
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      a6[k] = I.A[k];
-      c6[k] = I.C[k];
-    }
-#pragma unroll
-    for (int k = 0; k < 9; ++k) B[k] = I.B[k];
-    sym_planar(a6, planar, co, si);
-    sym_planar(c6, planar, co, si);
-    planar_rows(B, planar, co, si);
-    planar_cols(B, planar, co, si);
+    sym_planar(I.A, planar, co, si);
+    sym_planar(I.C, planar, co, si);
+    planar_rows(I.B, planar, co, si);
+    planar_cols(I.B, planar, co, si);
   } else {
+    FF a6[6], c6[6], B[9];
     sym_rotate(Rr.a, I.A, a6);
     sym_rotate(Rr.a, I.C, c6);
     gen_rotate(Rr.a, I.B, B);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      I.A[k] = a6[k];
+      I.C[k] = c6[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) I.B[k] = B[k];
   }
-  sym_expand(a6, A);
-  sym_expand(c6, Cm);
-  ABIF o;
-  shift_general(A, B, Cm, t, o);
-  return o;
+  FF BT[9];  // B' T
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    BT[3 * i] = ff_lin2(I.B[3 * i + 1], t.z, I.B[3 * i + 2], -t.y);
+    BT[3 * i + 1] = ff_lin2(I.B[3 * i], -t.z, I.B[3 * i + 2], t.x);
+    BT[3 * i + 2] = ff_lin2(I.B[3 * i], t.y, I.B[3 * i + 1], -t.x);
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    I.B[j] = ff_add(I.B[j], ff_lin2(symget(I.C, 1, j), -t.z, symget(I.C, 2, j), t.y));
+    I.B[3 + j] = ff_add(I.B[3 + j], ff_lin2(symget(I.C, 0, j), t.z, symget(I.C, 2, j), -t.x));
+    I.B[6 + j] = ff_add(I.B[6 + j], ff_lin2(symget(I.C, 0, j), -t.y, symget(I.C, 1, j), t.x));
+  }
+  const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const int i = ii[k], j = jj[k];
+    const FF bpt = j == 0 ? ff_lin2(I.B[3 * i + 1], t.z, I.B[3 * i + 2], -t.y)
+                          : (j == 1 ? ff_lin2(I.B[3 * i], -t.z, I.B[3 * i + 2], t.x)
+                                    : ff_lin2(I.B[3 * i], t.y, I.B[3 * i + 1], -t.x));
+    I.A[k] = ff_sub(I.A[k], ff_add(bpt, BT[3 * j + i]));
+  }
 }
 // I·(w, v) in FP32 from the rounded entries (the bias-force update needs only FP32).
 __device__ __forceinline__ SV<float> abi_mul_hi(const ABIF& I, const SV<float>& x) {
@@ -720,6 +738,11 @@ __device__ __forceinline__ SV<R> sv_r(const SV<double>& s) {
 // branch accumulators (and, whatever a lane writes there, every lane of the
 // pack must use the same element width: an FP32 row fills the first half of
 // the bytes of the FP64 row of the same index, the elements of lanes 0-15).
+// A body that can carry a contact wrench: contact points (count in bits 16-23
+// of topology word 1) or a cuboid collider (slot in bits 24-27).
+__device__ __forceinline__ bool has_wrench(uint32_t w1) {
+  return ((w1 >> 16) & 255u) != 0 || ((w1 >> W1_CUBOID_SHIFT) & 15u) != 0;
+}
 template <typename R>
 __device__ __forceinline__ int fd_row(const LaneCtx<R>& c) {
   return sizeof(R) == 8 ? c.L.F : c.L.FD;
@@ -750,8 +773,8 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
                                              bool have_tau, bool contacts) {
   using V = V3<R>;
   int st = 0;
-  ABIF carryI;
-  SVF carryP;
+  ABIF carryI{};
+  SVF carryP = svf_zero();
   int ctarget = -1;
   for (int b = c.nb - 1; b >= 0; --b) {
     const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
@@ -770,7 +793,8 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
       const V cm{c.t(tb + TD_INERTIA + 1), c.t(tb + TD_INERTIA + 2), c.t(tb + TD_INERTIA + 3)};
       pA = bias_force_ff(J, cm, c.t(tb + TD_INERTIA), vb.w, vb.v, (fl & BF_DIAG_INERTIA) != 0);
     }
-    if (contacts) pA = svf_add(pA, svf_from_double(load_svd(c, fd_row(c) + 6 * b)));  // − contact wrench
+    if (contacts && has_wrench(w1))  // − contact wrench (bodies with points or a cuboid collider)
+      pA = svf_add(pA, svf_from_double(load_svd(c, fd_row(c) + 6 * b)));
     ABIF IA = body_abi_ff(c, tb);
     if (fl & BF_BRANCH) {
       abi_add(IA, load_abi_ff(c, c.L.AI + ABI_D * b));
@@ -898,27 +922,33 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
       load_xf(c, b, planar, RrR, tr);
       const R co = planar >= 0 ? c.r(c.L.RF + 12 * b) : R(1);
       const R si = planar >= 0 ? c.r(c.L.RF + 12 * b + 1) : R(0);
-      if (type != 3) {
-        const ABIF Ip = abi_to_parent(IA, RrR, tr, planar, co, si);
-        if (pb == b - 1) {
-          carryI = Ip;
-        } else {
-          ABIF acc = load_abi_ff(c, c.L.AI + ABI_D * pb);
-          abi_add(acc, Ip);
-          store_abi_ff(c, c.L.AI + ABI_D * pb, acc);
-        }
-      } else if (pb == b - 1) {
-        carryI = ABIF{};  // floating joint below the parent: I^a = 0
-      }
+      // the bias force first: p^a is dead before the congruence's temporaries live
       const SVF fp = force_to_parent_ff(RrR, tr, pa, planar, co, si);
       if (pb == b - 1) {
         carryP = fp;
-        ctarget = pb;
       } else {
         store_svf(c, c.L.F + 6 * pb, svf_add(load_svf(c, c.L.F + 6 * pb), fp));
-        ctarget = -1;
+        carryP = svf_zero();
       }
+      if (type != 3) {
+        abi_to_parent_inplace(IA, RrR, tr, planar, co, si);
+        if (pb == b - 1) {
+          carryI = IA;
+        } else {
+          ABIF acc = load_abi_ff(c, c.L.AI + ABI_D * pb);
+          abi_add(acc, IA);
+          store_abi_ff(c, c.L.AI + ABI_D * pb, acc);
+          carryI = ABIF{};
+        }
+      } else {
+        carryI = ABIF{};  // floating joint: I^a = 0
+      }
+      ctarget = pb == b - 1 ? pb : -1;
     } else {
+      // every path writes both carries, so their previous values are dead once
+      // read at the top of the iteration (not held in registers through it)
+      carryI = ABIF{};
+      carryP = svf_zero();
       ctarget = -1;
     }
   }
@@ -1217,7 +1247,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       else store_sv(c, c.L.F + 6 * b, p);
     } else {
       store_sv(c, c.L.V + 6 * b, vb);  // passes 2 and 3 form c and p from it
-      if (contacts) store_svd(c, fd_row(c) + 6 * b, wc);
+      if (contacts && has_wrench(w1)) store_svd(c, fd_row(c) + 6 * b, wc);
     }
     if (fl & BF_BRANCH) {
       // accumulators for children other than b+1
@@ -1258,8 +1288,8 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
   if constexpr (sizeof(R) == 4) {
     st |= aba_inward_ff(c, q, v, tau, have_tau, contacts);
   } else {
-    ABI carryI;
-    SV<R> carryP;
+    ABI carryI{};
+    SV<R> carryP{zero, zero};
     int ctarget = -1;
     for (int b = c.nb - 1; b >= 0; --b) {
       const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
@@ -1405,9 +1435,10 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
             ABI acc = load_abi(c, c.L.AI + ABI_D * pb);
             abi_add(acc, Ip);
             store_abi(c, c.L.AI + ABI_D * pb, acc);
+            carryI = ABI{};
           }
-        } else if (pb == b - 1) {
-          carryI = ABI{};  // floating joint below the parent: I^a = 0
+        } else {
+          carryI = ABI{};  // floating joint: I^a = 0
         }
         // force to the parent frame: (Rr n + t × Rr f, Rr f)
         M3<R> RrR;
@@ -1420,9 +1451,13 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         } else {
           if (contacts) store_svd(c, fd_row(c) + 6 * pb, load_svd(c, fd_row(c) + 6 * pb) + sv_d(fp));
           else store_sv(c, c.L.F + 6 * pb, load_sv(c, c.L.F + 6 * pb) + fp);
+          carryP = SV<R>{zero, zero};
           ctarget = -1;
         }
       } else {
+        // every path writes both carries: their previous values are dead once read
+        carryI = ABI{};
+        carryP = SV<R>{zero, zero};
         ctarget = -1;
       }
     }
