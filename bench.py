@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -62,6 +63,12 @@ def parse():
     ap.add_argument("--serve-precisions", default="mixed,fp64")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM budget of the slot pool")
     ap.add_argument("--serve-algorithm", default="aba", choices=["aba", "crba"])
+    ap.add_argument("--serve-slo", action="store_true",
+                    help="serving target: isolated time per request, peak sustainable load, "
+                         "latency / isolated time at 50 %% of the peak")
+    ap.add_argument("--serve-load", type=float, default=0.5, help="fraction of the peak for --serve-slo")
+    ap.add_argument("--serve-peak-rate", type=float, default=20000.0,
+                    help="arrival rate (requests/s) of the saturating run of --serve-slo")
     ap.add_argument("--cuboids", action="store_true",
                     help="cuboid-collider workload: build_gripper batches (GJK/EPA jaw-cube "
                          "contacts) and independent collision queries")
@@ -591,63 +598,13 @@ def run_serve(args):
     runs = []
     for pname in args.serve_precisions.split(","):
         for rate in [float(r) for r in args.serve_rates.split(",")]:
-            rng = np.random.default_rng(args.seed)
-            n = int(rng.poisson(rate * args.serve_seconds))
-            t_arr = np.sort(rng.uniform(0.0, args.serve_seconds, n))
-            cfg = rng.choice(4, size=n, p=SERVE_MIX)
-            lo, hi = np.log(SERVE_HORIZON[0]), np.log(SERVE_HORIZON[1])
-            horizon = np.exp(rng.uniform(lo, hi, n)).astype(np.int64)
-            per = []
-            for c in range(4):
-                idx = np.nonzero(cfg == c)[0]
-                M, q0, v0, aux = Model.from_config(c, max(len(idx), 1), seed=args.seed + 17 * c)
-                per.append({"idx": idx, "M": M, "q0": q0, "v0": v0, "aux": aux, "next": 0,
-                            "t": t_arr[idx]})
+            t_arr, cfg, horizon, per = serve_stream(rate, args.serve_seconds, args.seed)
+            n = len(t_arr)
             S = Server(ctx, serve_classes(int(args.serve_budget_gb * 1e9), args.serve_algorithm),
                        precision=prec_of[pname],
                        chunk_steps=16, hbm_budget_bytes=int(args.serve_budget_gb * 1e9),
                        algorithm=gpb.ALGO_ABA if args.serve_algorithm == "aba" else gpb.ALGO_CRBA)
-            req_of = {}
-            lat = np.full(n, np.nan)
-            steps_done_total = 0
-            ticks = 0
-            tick_s = []
-            t0 = time.perf_counter()
-            deadline = args.serve_seconds + args.serve_drain
-            while True:
-                now = time.perf_counter() - t0
-                for c, P in enumerate(per):
-                    upto = int(np.searchsorted(P["t"], now, side="right"))
-                    if upto > P["next"]:
-                        a, b = P["next"], upto
-                        ids = S.submit(P["M"], a, b - a, P["q0"], P["v0"], dt=DT[c],
-                                       steps=horizon[P["idx"][a:b]], control=CONTROL[c],
-                                       tau=P["aux"] if c == 3 else None, seed=7 + c, kp=50.0,
-                                       kd=2.0, keys=0)
-                        for rid, r in zip(ids.tolist(), P["idx"][a:b].tolist()):
-                            req_of[rid] = r
-                        P["next"] = b
-                st = S.stats()
-                all_in = all(P["next"] == len(P["idx"]) for P in per)
-                if all_in and st["pending"] == 0 and st["active"] == 0:
-                    break
-                if now > deadline:
-                    break
-                if st["pending"] == 0 and st["active"] == 0:
-                    continue  # idle until the next arrival
-                ts = time.perf_counter()
-                S.tick()
-                ticks += 1
-                tick_s.append(time.perf_counter() - ts)
-                done = S.completed()
-                if done.size:
-                    tdone = time.perf_counter() - t0
-                    for rid in done.tolist():
-                        r = req_of.pop(rid)
-                        lat[r] = tdone - t_arr[r]
-                        steps_done_total += int(horizon[r])
-                    S.forget(done)
-            wall = time.perf_counter() - t0
+            lat, trace, wall = serve_run(S, gpb, t_arr, cfg, horizon, per, args.serve_seconds, args.serve_drain)
             ok = np.isfinite(lat)
             offered = float(rate * np.mean(horizon)) if n else 0.0
             runs.append({
@@ -659,10 +616,8 @@ def run_serve(args):
                 "latency_by_config_p50_s": {CONFIG_NAME[c]: float(np.median(lat[ok & (cfg == c)]))
                                             for c in range(4) if (ok & (cfg == c)).any()},
                 "offered_instance_steps_per_s": offered,
-                "achieved_instance_steps_per_s": steps_done_total / wall,
-                "wall_s": wall, "ticks": ticks,
-                "tick_ms": {"p50": 1e3 * float(np.median(tick_s)) if tick_s else None,
-                            "p99": 1e3 * float(np.quantile(tick_s, 0.99)) if tick_s else None},
+                "achieved_in_window_instance_steps_per_s": steps_rate(trace, 0.0, args.serve_seconds),
+                "wall_s": wall, "ticks": int(trace.shape[0]),
                 "pool_bytes": S.stats()["pool_bytes"]})
             S.close()
             print(json.dumps(runs[-1]), file=sys.stderr, flush=True)
@@ -673,6 +628,201 @@ def run_serve(args):
                        "arrival_window_s": args.serve_seconds, "hbm_budget_gb": args.serve_budget_gb,
                        "admission": "FIFO per slot class; pool sized to the budget"},
             "data": "synthetic (seeded)", "runs": runs}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
+def serve_stream(rate, seconds, seed):
+    """Poisson arrivals of the serving mix: arrival times, configuration, horizon
+    and the instance each request takes from its configuration's seeded model."""
+    from gpb import Model
+
+    rng = np.random.default_rng(seed)
+    n = int(rng.poisson(rate * seconds))
+    t_arr = np.sort(rng.uniform(0.0, seconds, n))
+    cfg = rng.choice(4, size=n, p=SERVE_MIX)
+    lo, hi = np.log(SERVE_HORIZON[0]), np.log(SERVE_HORIZON[1])
+    horizon = np.exp(rng.uniform(lo, hi, n)).astype(np.int64)
+    per = []
+    for c in range(4):
+        idx = np.nonzero(cfg == c)[0]
+        M, q0, v0, aux = Model.from_config(c, max(len(idx), 1), seed=seed + 17 * c)
+        per.append({"idx": idx, "M": M, "q0": q0, "v0": v0, "aux": aux, "next": 0, "t": t_arr[idx]})
+    return t_arr, cfg, horizon, per
+
+
+def serve_run(S, gpb, t_arr, cfg, horizon, per, window, drain):
+    """Feeds the stream to server S in real time for `window` seconds, then
+    runs at most `drain` seconds more.  Returns per-request
+    latency (NaN if not finished), the (time, instance-steps run) samples of
+    every tick and the wall time."""
+    n = len(t_arr)
+    req_of, lat = {}, np.full(n, np.nan)
+    trace = []
+    t0 = time.perf_counter()
+    while True:
+        now = time.perf_counter() - t0
+        for c, P in enumerate(per):
+            upto = int(np.searchsorted(P["t"], now, side="right"))
+            if upto > P["next"]:
+                a, b = P["next"], upto
+                ids = S.submit(P["M"], a, b - a, P["q0"], P["v0"], dt=DT[c], steps=horizon[P["idx"][a:b]],
+                               control=CONTROL[c], tau=P["aux"] if c == 3 else None, seed=7 + c, kp=50.0,
+                               kd=2.0, keys=0)
+                for rid, r in zip(ids.tolist(), P["idx"][a:b].tolist()):
+                    req_of[rid] = r
+                P["next"] = b
+        st = S.stats()
+        if all(P["next"] == len(P["idx"]) for P in per) and st["pending"] == 0 and st["active"] == 0:
+            break
+        if now > window + drain:
+            break
+        if st["pending"] == 0 and st["active"] == 0:
+            continue
+        S.tick()
+        tdone = time.perf_counter() - t0
+        trace.append((tdone, S.stats()["steps"]))
+        done = S.completed()
+        if done.size:
+            for rid in done.tolist():
+                r = req_of.pop(rid)
+                lat[r] = tdone - t_arr[r]
+            S.forget(done)
+    return lat, np.asarray(trace).reshape(-1, 2), time.perf_counter() - t0
+
+
+def steps_rate(trace, t_from, t_to):
+    """Instance-steps per second run between two times of a serve_run trace."""
+    if trace.shape[0] < 2:
+        return 0.0
+    s0, s1 = np.interp([t_from, t_to], trace[:, 0], trace[:, 1])
+    return float((s1 - s0) / max(t_to - t_from, 1e-9))
+
+
+def run_serve_slo(args):
+    """The serving target: p99 latency against the isolated-request time at a
+    fraction (default 50 %) of the peak sustainable load.
+
+    1. Isolated time: single requests on an empty server — per configuration
+       the time of a short and a long horizon (chains at five DOF counts), a
+       linear model a + b·H per configuration (chains: b interpolated in DOF).
+    2. Peak: arrivals far above what the GPU can run (offered 20× the measured
+       throughput), so that the running set only grows; the instance-steps run
+       (gpb_server_stats.steps) in the second half of the window over that
+       half's length is the saturated throughput.
+    3. Load: Poisson arrivals at load × peak ÷ mean horizon for the arrival
+       window, then drained; per request the slowdown latency ÷ isolated time.
+    Throughput of the load run counts the instance-steps run inside the
+    arrival window only."""
+    import torch
+
+    torch.cuda.set_device(0)
+    import gpb
+    from gpb import Model
+    from gpb.serve import Server
+
+    ctx = gpb.Context(0)
+    prec_of = {"fp64": gpb.FP64, "mixed": gpb.MIXED}
+    algo = gpb.ALGO_ABA if args.serve_algorithm == "aba" else gpb.ALGO_CRBA
+    budget = int(args.serve_budget_gb * 1e9)
+    mean_h = (SERVE_HORIZON[1] - SERVE_HORIZON[0]) / math.log(SERVE_HORIZON[1] / SERVE_HORIZON[0])
+    out_runs = []
+    for pname in args.serve_precisions.split(","):
+        def server():
+            return Server(ctx, serve_classes(budget, args.serve_algorithm), precision=prec_of[pname],
+                          chunk_steps=16, hbm_budget_bytes=budget, algorithm=algo)
+
+        # 1. isolated times
+        S = server()
+        iso = {}
+        H_lo, H_hi = 200, 4000
+        probe = {0: [None], 1: [2, 13, 25, 37, 48], 2: [None], 3: [None]}
+        for c in range(4):
+            M, q0, v0, aux = Model.from_config(c, 256, seed=args.seed + 5 * c)
+            nv = np.diff(M.offsets()[1])
+            for dof in probe[c]:
+                j = 0 if dof is None else int(np.argmin(np.abs(nv - dof)))
+                T = []
+                for H in (H_lo, H_hi):
+                    t0 = time.perf_counter()
+                    S.submit(M, j, 1, q0, v0, dt=DT[c], steps=H, control=CONTROL[c],
+                             tau=aux if c == 3 else None, seed=7 + c, kp=50.0, kd=2.0, keys=0)
+                    while True:
+                        S.tick()
+                        d = S.completed()
+                        if d.size:
+                            S.forget(d)
+                            break
+                    T.append(time.perf_counter() - t0)
+                b = (T[1] - T[0]) / (H_hi - H_lo)
+                iso[(c, int(nv[j]) if dof is not None else None)] = (T[0] - b * H_lo, b)
+        S.close()
+        chain_dofs = sorted(k[1] for k in iso if k[0] == 1)
+
+        def t_iso(c, dof, H):
+            if c != 1:
+                a, b = iso[(c, None)]
+                return a + b * H
+            a = np.interp(dof, chain_dofs, [iso[(1, d)][0] for d in chain_dofs])
+            b = np.interp(dof, chain_dofs, [iso[(1, d)][1] for d in chain_dofs])
+            return a + b * H
+
+        # 2. peak sustainable throughput (closed loop: the queue never empties)
+        w = max(args.serve_seconds, 10.0)
+        t_arr, cfg, horizon, per = serve_stream(args.serve_peak_rate, w, args.seed + 1)
+        S = server()
+        _, trace, _ = serve_run(S, gpb, t_arr, cfg, horizon, per, w, 0.0)
+        S.close()
+        peak = steps_rate(trace, w / 2, min(w, trace[-1, 0]))
+
+        # 3. the load run at args.serve_load of the peak
+        rate = args.serve_load * peak / mean_h
+        t_arr, cfg, horizon, per = serve_stream(rate, args.serve_seconds, args.seed)
+        dof = np.zeros(len(t_arr), np.int64)
+        for c, P in enumerate(per):
+            nvs = np.diff(P["M"].offsets()[1])
+            dof[P["idx"]] = nvs[:len(P["idx"])]
+        S = server()
+        lat, trace, wall = serve_run(S, gpb, t_arr, cfg, horizon, per, args.serve_seconds, args.serve_drain)
+        S.close()
+        ok = np.isfinite(lat)
+        tiso = np.array([t_iso(int(cfg[r]), int(dof[r]), int(horizon[r])) for r in range(len(t_arr))])
+        slow = lat / tiso
+
+        def q(x, p):
+            return float(np.quantile(x, p)) if x.size else None
+
+        by_cfg = {}
+        for c in range(4):
+            m = ok & (cfg == c)
+            by_cfg[CONFIG_NAME[c]] = {"requests": int(m.sum()), "latency_p99_s": q(lat[m], 0.99),
+                                      "isolated_p99_s": q(tiso[m], 0.99),
+                                      "slowdown_p50": q(slow[m], 0.5), "slowdown_p99": q(slow[m], 0.99)}
+        run = {"precision": pname, "peak_instance_steps_per_s": peak, "peak_arrival_rate_req_s": args.serve_peak_rate,
+               "load_fraction": args.serve_load,
+               "rate_req_s": rate, "requests": int(len(t_arr)), "completed": int(ok.sum()),
+               "censored": int((~ok).sum()),
+               "latency_s": {"p50": q(lat[ok], 0.5), "p99": q(lat[ok], 0.99)},
+               "isolated_s": {"p50": q(tiso[ok], 0.5), "p99": q(tiso[ok], 0.99)},
+               "p99_over_isolated_p99": (q(lat[ok], 0.99) / q(tiso[ok], 0.99)) if ok.any() else None,
+               "slowdown": {"p50": q(slow[ok], 0.5), "p99": q(slow[ok], 0.99), "max": float(slow[ok].max())
+                            if ok.any() else None,
+                            "definition": "latency ÷ the same request's isolated time (class, DOF, horizon)"},
+               "by_config": by_cfg,
+               "achieved_in_window_instance_steps_per_s": steps_rate(trace, 0.0, args.serve_seconds),
+               "offered_instance_steps_per_s": rate * mean_h,
+               "isolated_model": {f"{CONFIG_NAME[k[0]]}{'' if k[1] is None else ' n=' + str(k[1])}":
+                                  {"fixed_s": a, "per_step_s": b} for k, (a, b) in iso.items()},
+               "wall_s": wall}
+        out_runs.append(run)
+        print(json.dumps(run), file=sys.stderr, flush=True)
+    line = {"metric": "serving p99 latency over the isolated-request time at a fraction of peak load",
+            "unit": "ratio", "n_gpus": 1, "higher_is_better": False,
+            "config": {"workload": "serving mix acrobot/chain/cube/quadruped = 40/30/20/10 %",
+                       "horizon_steps": "log-uniform [100, 50000]", "arrival_window_s": args.serve_seconds,
+                       "hbm_budget_gb": args.serve_budget_gb, "algorithm": args.serve_algorithm},
+            "data": "synthetic (seeded)", "runs": out_runs}
     print(json.dumps(line))
     ctx.close()
     return 0
@@ -984,6 +1134,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference_cuboids(args) if args.cuboids else run_reference(args)
+    if args.serve_slo:
+        return run_serve_slo(args)
     if args.serve:
         return run_serve(args)
     if args.cuboids:

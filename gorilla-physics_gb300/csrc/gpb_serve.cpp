@@ -88,6 +88,8 @@ struct Request {
   std::vector<double> q, v, tau;
   gpb_request req{};
   std::chrono::steady_clock::time_point t_submit;
+  int64_t left = 0;   // steps not yet launched (host count, for gpb_server_stats.steps)
+  int64_t chunk = 0;  // steps per tick of its class
 };
 
 struct Result {
@@ -147,7 +149,7 @@ struct gpb_server {
   std::unordered_map<uint64_t, Result> results;
   std::vector<uint64_t> unread;
   uint64_t next_id = 1;
-  int64_t ticks = 0, completed = 0, pool_bytes = 0;
+  int64_t ticks = 0, completed = 0, pool_bytes = 0, steps_run = 0;
   ScatterTable table{};
 };
 
@@ -552,6 +554,8 @@ extern "C" int gpb_server_tick(gpb_server* S, int32_t* completed_now) {
     j.integrator = R.req.integrator;
     j.tau_mode = (R.req.control == GPB_CONTROL_HOST_TAU && !R.tau.empty()) ? 1 : 0;
     j.chunk = C.caps.chunk_steps;
+    R.left = R.req.steps;
+    R.chunk = C.caps.chunk_steps > 0 ? C.caps.chunk_steps : S->opts.chunk_steps;
     uint64_t words[LANE_JOB_WORDS];
     std::memcpy(words, &j, sizeof(j));
     for (int w = 0; w < LANE_JOB_WORDS; ++w) sink.put(T_JOBS, (int64_t)slot * LANE_JOB_WORDS + w, words[w]);
@@ -603,6 +607,12 @@ extern "C" int gpb_server_tick(gpb_server* S, int32_t* completed_now) {
   p.K = S->opts.chunk_steps;
   p.precision = S->opts.precision;
   p.dt = 1.0;  // per-slot values come from the jobs
+  for (auto& kv : S->running) {  // every admitted request runs min(chunk, left) steps
+    Request& R = kv.second;
+    const int64_t k = std::min(R.chunk, R.left);
+    R.left -= k;
+    S->steps_run += k;
+  }
   CUDA_TRY(cudaEventRecord(S->ctx->ev0, s));
   CUDA_TRY(launch_simulate(db, p, S->ctx->num_sms, 0, s));
   CUDA_TRY(cudaEventRecord(S->ctx->ev1, s));
@@ -672,6 +682,7 @@ extern "C" int gpb_server_tick(gpb_server* S, int32_t* completed_now) {
     oq += R.info.nq;
     ov += R.info.nv;
     std::memcpy(&res.steps_done, outw.data() + oj + k, 8);
+    S->steps_run += res.steps_done - (R.req.steps - R.left);  // exact once retired (a failed job stops early)
     res.status = (int32_t)st32[k];
     res.latency_s = std::chrono::duration<double>(now - R.t_submit).count();
     S->results.emplace(id, std::move(res));
@@ -726,5 +737,6 @@ extern "C" int gpb_server_stats_get(const gpb_server* S, gpb_server_stats* st) {
   st->slots = (int64_t)S->slot_req.size();
   st->ticks = S->ticks;
   st->pool_bytes = S->pool_bytes;
+  st->steps = S->steps_run;
   return GPB_OK;
 }

@@ -104,7 +104,7 @@ class GpbRequest(C.Structure):
 
 
 class GpbServerStats(C.Structure):
-    _fields_ = [(n, C.c_int64) for n in ("pending", "active", "completed", "slots", "ticks", "pool_bytes")]
+    _fields_ = [(n, C.c_int64) for n in ("pending", "active", "completed", "slots", "ticks", "pool_bytes", "steps")]
 
 
 # (name, restype, argtypes) of every exported entry point

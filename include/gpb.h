@@ -470,8 +470,10 @@ typedef struct gpb_request {
   int32_t key;              /* instance number of the open-loop draw (0 = as a batch of one) */
 } gpb_request;
 
+/* steps: instance-steps run so far (exact for retired requests, counted from
+ * the chunks launched for running ones). */
 typedef struct gpb_server_stats {
-  int64_t pending, active, completed, slots, ticks, pool_bytes;
+  int64_t pending, active, completed, slots, ticks, pool_bytes, steps;
 } gpb_server_stats;
 
 /* Host-only sizing: device bytes of one pack of each class and the packs each
