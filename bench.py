@@ -205,12 +205,11 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from gpb import Model
-
-    M, q0, v0, aux = Model.from_config(args.config, args.instances, seed=args.seed)
     import oracle
 
     oracle.build()
+    # inputs from the CPU build of the workload generator: this arm loads no CUDA library
+    M, q0, v0, aux = oracle.from_config(args.config, args.instances, seed=args.seed)
     threads = os.cpu_count() or 1
     qo, vo, _ = M.offsets()
     sample = min(M.n, 4096)

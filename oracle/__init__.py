@@ -19,7 +19,12 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 LIB = HERE / "liboracle.so"
 SRC = HERE / "gpb_oracle.cpp"
-SOURCES = (SRC, HERE / "collision.cpp", HERE / "socp.cpp")
+# The seeded workload generator (the benchmark configurations' mechanisms and
+# initial states) is the package's own source file, compiled here for the CPU so
+# that the reference arm of the benchmark builds its inputs without loading the
+# CUDA library; tests check that both builds produce identical tables.
+CONFIGS_SRC = REPO / "gorilla-physics_gb300" / "csrc" / "gpb_configs.cpp"
+SOURCES = (SRC, HERE / "collision.cpp", HERE / "socp.cpp", CONFIGS_SRC)
 
 P_f64 = C.POINTER(C.c_double)
 P_i64 = C.POINTER(C.c_int64)
@@ -30,11 +35,13 @@ LU, CHOLESKY = 0, 1
 
 def build(force: bool = False) -> Path:
     """g++ -O2 -ffp-contract=off (x86 and Arm agree bit for bit)."""
-    deps = [*SOURCES, HERE / "collision.h", HERE / "socp.h", REPO / "include/gpb.h"]
+    deps = [*SOURCES, HERE / "collision.h", HERE / "socp.h", REPO / "include/gpb.h",
+            CONFIGS_SRC.parent / "gpb_rng.h", Path(__file__)]
     if force or not LIB.exists() or LIB.stat().st_mtime < max(p.stat().st_mtime for p in deps):
         tmp = LIB.with_suffix(".so.tmp")
         subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
-                        "-I", str(REPO / "include"), *map(str, SOURCES), "-o", str(tmp), "-lpthread"],
+                        "-I", str(REPO / "include"), "-I", str(CONFIGS_SRC.parent), *map(str, SOURCES),
+                        "-o", str(tmp), "-lpthread"],
                        check=True)
         os.replace(tmp, LIB)
     return LIB
@@ -65,6 +72,10 @@ def lib():
         L.oracle_simulate.argtypes = [vp, C.c_int64, P_f64, P_f64, C.c_double, C.c_int64,
                                       C.c_int64, C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_int,
                                       C.c_double, C.c_double, C.c_double, P_f64, C.c_int64, P_f64]
+        L.gpb_config_sizes.argtypes = [C.c_int, C.c_int64, C.c_uint32] + [P_i64] * 5
+        L.gpb_config_build.argtypes = [C.c_int, C.c_int64, C.c_uint32, C.c_int, P_i32, P_i32, P_i32, P_f64,
+                                       P_f64, P_f64, P_f64, P_i32, P_i32, P_f64, P_i32, P_f64, P_i32,
+                                       P_f64, P_f64, P_f64]
         L.oracle_simulate_batch.argtypes = [vp, C.c_int64, C.c_int64, P_i64, P_i64, P_f64, P_f64,
                                             C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_int,
                                             C.c_int, C.c_uint32, C.c_int, C.c_double, C.c_double,
@@ -227,3 +238,37 @@ def simulate_batch(model, q_all, v_all, dt, K, integrator=0, solver=LU, control=
                                      sigma, kp, kd, _p(c), threads)
     if rc:
         raise ValueError("oracle: malformed model")
+
+
+def from_config(config, n, seed=0, contact_model=1):
+    """The benchmark configuration's seeded mechanisms and initial state, built
+    by the CPU compilation of the workload generator (no CUDA library is
+    loaded).  Returns (model, q0, v0, aux) like gpb.Model.from_config."""
+    from gpb.model import Model  # the table container only
+
+    L = lib()
+    sz = [C.c_int64() for _ in range(5)]
+    rc = L.gpb_config_sizes(config, n, seed, *[C.byref(x) for x in sz])
+    if rc:
+        raise ValueError(f"oracle.from_config: bad configuration {config}")
+    nj, nc, nh, nq, nv = (x.value for x in sz)
+    a = dict(joint_offset=np.zeros(n + 1, np.int32), joint_type=np.zeros(nj, np.int32),
+             joint_parent=np.zeros(nj, np.int32), joint_iso=np.zeros(7 * nj), joint_axis=np.zeros(3 * nj),
+             joint_spring=np.zeros(2 * nj), body_inertia=np.zeros(10 * nj),
+             contact_offset=np.zeros(n + 1, np.int32), contact_body=np.zeros(max(nc, 1), np.int32),
+             contact_params=np.zeros(max(6 * nc, 1)), halfspace_offset=np.zeros(n + 1, np.int32),
+             halfspace_params=np.zeros(max(8 * nh, 1)), contact_model=np.zeros(n, np.int32))
+    q0, v0, aux = np.zeros(max(nq, 1)), np.zeros(max(nv, 1)), np.zeros(max(nv, 1))
+    i32 = lambda x: x.ctypes.data_as(P_i32)
+    f64 = lambda x: x.ctypes.data_as(P_f64)
+    rc = L.gpb_config_build(config, n, seed, contact_model, i32(a["joint_offset"]), i32(a["joint_type"]),
+                            i32(a["joint_parent"]), f64(a["joint_iso"]), f64(a["joint_axis"]),
+                            f64(a["joint_spring"]), f64(a["body_inertia"]), i32(a["contact_offset"]),
+                            i32(a["contact_body"]), f64(a["contact_params"]), i32(a["halfspace_offset"]),
+                            f64(a["halfspace_params"]), i32(a["contact_model"]), f64(q0), f64(v0), f64(aux))
+    if rc:
+        raise ValueError(f"oracle.from_config: build failed ({rc})")
+    a["contact_body"] = a["contact_body"][:nc]
+    a["contact_params"] = a["contact_params"][:6 * nc]
+    a["halfspace_params"] = a["halfspace_params"][:8 * nh]
+    return Model(**a), q0[:nq], v0[:nv], aux[:nv]

@@ -54,3 +54,32 @@ def test_reference_arm_prints_its_line():
         assert k in line
     assert line["value"] > 0 and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_loads_no_cuda_library():
+    """The reference arm builds its inputs with the CPU build of the workload
+    generator: running it maps neither libgpb.so nor the CUDA runtime."""
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '1', "
+            "'--instances', '512']; import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPS', 'libgpb.so' in maps, 'libcudart' in maps)")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip().splitlines()[-1] == "MAPS False False"
+
+
+def test_oracle_workload_generator_matches_the_library():
+    """oracle.from_config (CPU build) and gpb.Model.from_config (libgpb.so) give
+    identical tables and initial states for every configuration."""
+    import numpy as np
+
+    import oracle
+    from gpb import Model
+
+    for config in range(4):
+        A = Model.from_config(config, 300, seed=11)
+        B = oracle.from_config(config, 300, seed=11)
+        for x, y in zip(A[1:], B[1:]):
+            np.testing.assert_array_equal(x, y)
+        for name in Model.FIELDS:
+            np.testing.assert_array_equal(getattr(A[0], name), getattr(B[0], name), err_msg=name)
