@@ -139,6 +139,50 @@ def test_oracle_box_pusher(built):
     assert box[0] > 2.0
 
 
+def test_oracle_box_pusher_cause(built):
+    """Why the restated box pusher stops short of x > 3 (the cause, shown).
+
+    The pusher's face (0.2 m wide, 1.75 m tall) covers the whole height of the
+    box's back face, so their contact is a 0.2 × 0.5 m patch, but
+    CollisionDetector returns one contact point (EPA's closest point of the
+    Minkowski difference, src/collision/epa.rs), which for a face-face contact
+    lands on a corner of the patch.  Along the oracle's trajectory the point sits
+    on the box's top or bottom edge in most contact steps, never near the face's
+    centre, and flips between the two edges: the single off-centre push tips
+    and yaws the box (about 1 rad by the time it slides off the pusher at
+    x ≈ 2.45), so it never reaches x = 3.  The reference runs the same
+    single-point contact, and its own test notes that it depends on friction
+    ("needs friction mu to be < 1.0")."""
+    from scipy.spatial.transform import Rotation
+
+    M = Model.from_mechanisms([builders.build_pusher()])
+    q = np.array([0, 0, 0, 0, 0, 1, 0, 0, 0], float)
+    v = np.zeros(8)
+    dt = 1.0 / 120.0
+    zrel, yaw_hit, box_x = [], [], []
+    for _ in range(int(5.0 / dt)):
+        Rz = Rotation.from_euler("z", q[0])
+        pc = np.array([0, 0, 2.0]) + Rz.apply([0.35 + q[1], 0, -1.125])  # pusher centre
+        bc = q[6:9] + np.array([1.2, 0, 0.25])                            # box centre
+        r, _, cb = oracle.collide_cuboids(np.r_[Rz.as_quat(), pc][None], [[0.2, 0.2, 1.75]],
+                                          np.r_[q[2:6], bc][None], [[0.5, 0.5, 0.5]])
+        if r[0] == oracle.COL_HIT:
+            zrel.append(cb[0][2] - bc[2])
+            yaw_hit.append(Rotation.from_quat(q[2:6]).as_euler("xyz")[2])
+            box_x.append(bc[0])
+        qd = 3.0 - q[1]
+        vt = math.copysign(10.0 * min(abs(qd), 0.1), qd)
+        tau = np.array([0, 20.0 * (vt - v[1]), 0, 0, 0, 0, 0, 0])
+        q, v, st = oracle.step(M, 0, q, v, dt, tau, VS)
+        assert st == 0
+    z = np.array(zrel)
+    assert z.size > 50
+    assert np.mean(np.abs(z) >= 0.24) > 0.75       # on the top or bottom edge (half height 0.25)
+    assert np.all(np.abs(z) > 0.1)                 # never near the middle of the face
+    assert np.sum(np.diff(np.sign(z)) != 0) >= 10  # flips between the two edges
+    assert abs(yaw_hit[-1]) > 0.5 and box_x[-1] < 3.0
+
+
 def cube_states(rng, n):
     """Cubes of side 0.4-1.0 m tilted by up to 0.2 rad, the lowest corners
     0-2 mm below the ground, random velocities (1-4 corner contacts)."""
