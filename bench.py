@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--mix-chains", type=int, default=0,
                     help="also step this many serial chains in the same batch (one control law for all)")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
+    ap.add_argument("--warps-per-sm", type=int, default=0,
+                    help="resident warps per SM of the step kernel (0: the autotuner chooses)")
     ap.add_argument("--precision", default="all", choices=["all", "fp64", "mixed", "refined"])
     ap.add_argument("--serve", action="store_true",
                     help="serving mix instead: Poisson arrivals, latency percentiles per rate")
@@ -368,7 +370,11 @@ def run_gpu(args):
         B.update(q0, v0)
         B.clear_status()
         # launch shape for this workload and form (short trials, state restored)
-        w, c = B.autotune(dt, 0, prec, trial_steps=10, **kw)
+        if args.warps_per_sm:
+            B.set_launch(args.warps_per_sm)
+            w, c = args.warps_per_sm, 0
+        else:
+            w, c = B.autotune(dt, 0, prec, trial_steps=10, **kw)
         launch[name] = {"warps_per_sm": w, "coop_min_dof": c}
         if args.warmup:
             B.simulate_steps(args.warmup, dt, 0, prec, step0=0, **kw)

@@ -38,6 +38,11 @@ def test_ncu_tables_hold_what_bench_reads():
     m = t["serial-chain"]["mixed"]
     assert m["dram_bytes_per_instance_step"] > 0 and m["warp_instructions_per_instance_step"] > 0
     assert "capture" in m
+    # captured on the kernel sources in the tree (bench.py ignores a table of other sources)
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert m["source_sha16"] == bench.kernel_source_hash()
     v = json.loads((ROOT / "profiles" / "vstep_work.json").read_text())
     assert v["fp64_flops_per_instance_step"] > 0 and "source" in v
     c = json.loads((ROOT / "profiles" / "collision_work.json").read_text())
