@@ -586,7 +586,9 @@ def serve_classes(budget_bytes, algorithm="aba"):
     for (s, share), nb in zip(specs, nbytes):
         c = cost(s[0], s[2], s[3])
         # concurrent slots ∝ share × residence time (∝ cost); bytes ∝ slots × pack bytes
-        out.append(SlotClass(*s, weight=share * c * float(nb), chunk_steps=max(1, int(round(16 * cmax / c)))))
+        # acrobots and chains are planar chains: their classes run the specialised passes
+        out.append(SlotClass(*s, weight=share * c * float(nb), chunk_steps=max(1, int(round(16 * cmax / c))),
+                             planar_only=s[3] == 0))
     return out
 
 

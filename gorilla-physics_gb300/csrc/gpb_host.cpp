@@ -97,6 +97,7 @@ int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
     return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": body count outside [0, 64]");
   I.nq = I.nv = 0;
   I.chain = true;
+  I.planar = true;
   uint64_t sig = 1469598103934665603ull;
   for (int b = 0; b < I.nb; ++b) {
     int t = m->joint_type[I.j0 + b], p = m->joint_parent[I.j0 + b];
@@ -108,6 +109,15 @@ int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
       return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": joint " + std::to_string(b + 1) +
                                    " has parent " + std::to_string(p) + " (must be < its own number)");
     if (p != b) I.chain = false;
+    {
+      const double* iso = m->joint_iso + 7 * (size_t)(I.j0 + b);
+      const double* ax = m->joint_axis + 3 * (size_t)(I.j0 + b);
+      const int nz = (ax[0] != 0.0) + (ax[1] != 0.0) + (ax[2] != 0.0);
+      const double amax = std::max(std::fabs(ax[0]), std::max(std::fabs(ax[1]), std::fabs(ax[2])));
+      if (t != GPB_JOINT_REVOLUTE || p != b || !(iso[0] == 0.0 && iso[1] == 0.0 && iso[2] == 0.0 && iso[3] == 1.0) ||
+          nz != 1 || amax != 1.0)
+        I.planar = false;
+    }
     I.nq += joint_nq(t);
     I.nv += joint_nv(t);
     sig = (sig ^ (uint64_t)(t * 131 + p)) * 1099511628211ull;
@@ -140,6 +150,7 @@ int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
                                    std::to_string(GPB_MAX_CUBOIDS) + " cuboid colliders");
   }
   I.mvs = I.nc * I.nh + I.nu * (I.nu - 1) / 2;
+  if (I.nc > 0 || I.nu > 0) I.planar = false;
   sig = (sig ^ (uint64_t)(I.nc * 7 + I.nh + 1000 * I.nu)) * 1099511628211ull;
   I.sig = sig;
   return GPB_OK;
@@ -190,6 +201,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
     std::memset(&P, 0, sizeof(P));
     P.count = (int32_t)std::min<int64_t>(LANES, n - p * LANES);
     P.chain = 1;
+    P.planar = 1;
     P.minnv = GPB_MAX_DOF;
     for (int l = 0; l < P.count; ++l) {
       const InstInfo& I = info[order[p * LANES + l]];
@@ -202,6 +214,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
       P.mvs = std::max(P.mvs, I.mvs);
       P.minnv = std::min(P.minnv, I.nv);
       if (!I.chain) P.chain = 0;
+      if (!I.planar) P.planar = 0;
     }
     P.topo = rt;
     P.ctc = rc;

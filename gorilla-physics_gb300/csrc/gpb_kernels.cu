@@ -68,6 +68,7 @@ struct RealTopo<float> {
 template <typename R>
 struct LaneCtx {
   int lane, nb, nq, nv, nc, nh, model, chain;
+  int planar;   // every lane of the pack is a planar chain (PackDesc::planar)
   int nu;       // cuboid colliders (slots 1..nu in body order)
   int springs;  // prismatic springs act (off for Articulated::free_velocity)
   int allx;     // keep every body's world pose in X (velocity stepping)
@@ -959,7 +960,9 @@ struct EvalFP64 {
   int algo;  // GPB_ALGO_CRBA / GPB_ALGO_ABA
   __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
                             Col<double> cf = Col<double>{nullptr}, bool want_cf = false) const {
-    if (algo == 1) return lane_aba<double>(c, q, v, t, ht, x, cf, want_cf);
+    if (algo == 1)
+      return c.planar ? lane_aba<double, true>(c, q, v, t, ht, x, cf, want_cf)
+                      : lane_aba<double, false>(c, q, v, t, ht, x, cf, want_cf);
     return lane_dynamics<double, double>(c, q, v, t, ht, x, cf, want_cf);
   }
 };
@@ -968,7 +971,9 @@ struct EvalMixed {  // CRBA: FP32 sweeps and fill, FP64 Cholesky when n > 12; AB
   int algo;
   __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
                             Col<double> cf = Col<double>{nullptr}, bool want_cf = false) const {
-    if (algo == 1) return lane_aba<float>(c, q, v, t, ht, x, cf, want_cf);
+    if (algo == 1)
+      return c.planar ? lane_aba<float, true>(c, q, v, t, ht, x, cf, want_cf)
+                      : lane_aba<float, false>(c, q, v, t, ht, x, cf, want_cf);
     if (c.nv <= 12) return lane_dynamics<float, float>(c, q, v, t, ht, x, cf, want_cf);
     return lane_dynamics<float, double>(c, q, v, t, ht, x, cf, want_cf);
   }
@@ -1055,6 +1060,7 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   c.model = li[6 * LANES];
   c.nu = b.plain ? 0 : li[7 * LANES];  // free_velocity: no colliders
   c.chain = pd.chain;
+  c.planar = pd.planar;
   c.springs = b.plain ? 0 : 1;
   c.allx = 0;
   c.grav = b.gravity;

@@ -253,6 +253,7 @@ extern "C" int gpb_server_create(gpb_ctx* ctx, const gpb_server_opts* o, gpb_ser
       P.nh = C.caps.max_halfspaces;
       P.nu = C.caps.max_cuboids;
       P.chain = 0;
+      P.planar = C.caps.planar_only ? 1 : 0;
       P.topo = rt;
       P.ctc = rc;
       P.hs = rh;
@@ -389,15 +390,19 @@ extern "C" int gpb_server_submit(gpb_server* S, const gpb_model* m, int64_t firs
       return fail(GPB_E_INVAL, "gpb_server_submit: request " + std::to_string(k) +
                                    ": dt > 0, steps >= 1 and a known integrator / control are required "
                                    "(velocity stepping is not served)");
-    // smallest class that fits
+    // smallest class that fits; a planar chain takes a planar-only class first.
+    // The choice depends on the request alone, so its path (and its bits) do too.
     int best = -1;
-    for (int c = 0; c < (int)S->classes.size(); ++c) {
-      const gpb_slot_class& cap = S->classes[c].caps;
-      if (S->classes[c].npacks == 0 || R.info.nb > cap.max_bodies || R.info.nq > cap.max_q ||
-          R.info.nv > cap.max_v || R.info.nc > cap.max_contacts || R.info.nh > cap.max_halfspaces ||
-          R.info.nu > cap.max_cuboids)
-        continue;
-      if (best < 0 || S->classes[c].pack_bytes < S->classes[best].pack_bytes) best = c;
+    for (int pass = R.info.planar ? 0 : 1; pass < 2 && best < 0; ++pass) {
+      for (int c = 0; c < (int)S->classes.size(); ++c) {
+        const gpb_slot_class& cap = S->classes[c].caps;
+        if ((cap.planar_only != 0) != (pass == 0)) continue;
+        if (S->classes[c].npacks == 0 || R.info.nb > cap.max_bodies || R.info.nq > cap.max_q ||
+            R.info.nv > cap.max_v || R.info.nc > cap.max_contacts || R.info.nh > cap.max_halfspaces ||
+            R.info.nu > cap.max_cuboids)
+          continue;
+        if (best < 0 || S->classes[c].pack_bytes < S->classes[best].pack_bytes) best = c;
+      }
     }
     if (best < 0)
       return fail(GPB_E_RANGE, "gpb_server_submit: instance " + std::to_string(i) + " fits no slot class");

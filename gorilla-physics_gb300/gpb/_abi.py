@@ -73,6 +73,7 @@ class GpbSlotClass(C.Structure):
         ("packs", C.c_int32),
         ("chunk_steps", C.c_int32),
         ("max_cuboids", C.c_int32),
+        ("planar_only", C.c_int32),
     ]
 
 

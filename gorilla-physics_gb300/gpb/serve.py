@@ -32,11 +32,12 @@ class SlotClass:
     packs: int = 0       # packs of 32 slots
     chunk_steps: int = 0  # steps per tick of this class (0: the server's chunk_steps)
     max_cuboids: int = 0  # cuboid colliders per instance
+    planar_only: bool = False  # planar chains only (their packs run the specialised passes)
 
     def struct(self) -> _abi.GpbSlotClass:
         return _abi.GpbSlotClass(self.max_bodies, self.max_q, self.max_v, self.max_contacts,
                                  self.max_halfspaces, float(self.weight), int(self.packs),
-                                 int(self.chunk_steps), int(self.max_cuboids))
+                                 int(self.chunk_steps), int(self.max_cuboids), int(bool(self.planar_only)))
 
 
 # numpy image of gpb_request (same field order and alignment)

@@ -434,7 +434,9 @@ double gpb_open_loop_tau(uint32_t seed, int64_t instance, int64_t block, int32_t
  * request run alone, bit for bit.
  *
  * The pool is divided into slot classes (capacities in bodies, q, v, contacts,
- * half-spaces).  Each request goes to the smallest class it fits; it waits in
+ * half-spaces, and whether the class takes planar chains only).  Each request
+ * goes to the smallest class it fits (planar-only classes first for a planar
+ * chain); it waits in
  * a FIFO queue until that class has a free slot (the admission limit is the
  * HBM budget the pool was sized to).  A server is single-threaded like its
  * context.
@@ -447,6 +449,12 @@ typedef struct gpb_slot_class {
   int32_t packs;  /* packs of 32 slots of a fixed class (weight 0) */
   int32_t chunk_steps; /* steps per tick of this class's requests (0 = the server's) */
   int32_t max_cuboids; /* cuboid colliders per instance (0..GPB_MAX_CUBOIDS) */
+  int32_t planar_only; /* 1: only planar chains (revolute joints about ±x/±y/±z with
+                          identity joint rotations, each body the child of the previous,
+                          no contacts, colliders or springs); its packs run the
+                          articulated-body passes specialised for them.  A planar chain
+                          goes to the smallest planar-only class it fits, else to the
+                          smallest other class. */
 } gpb_slot_class;
 
 typedef struct gpb_server_opts {

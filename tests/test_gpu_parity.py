@@ -153,12 +153,16 @@ def _pack_kinds(M):
 @pytest.mark.parametrize("precision", [gpb.FP64, gpb.MIXED, gpb.MIXED_REFINED])
 def test_mixed_contact_batches(ctx, algorithm, precision):
     """Quadrupeds (contacts) batched with serial chains (none), so that packs
-    hold both kinds: every instance's q̈ is bit-identical to the one it gets in
-    a batch of its own kind (a lane reads and writes nothing of its
-    neighbours), MIXED with the articulated-body algorithm stays within 1e-5 of
-    FP64 (relative to max(|q̈|, 1)), MIXED_REFINED within 1e-6, and no status
-    bit is set.  A mixed pack once let the FP32 bias forces of its
-    chain lanes overwrite the FP64 bias forces of its contact lanes."""
+    hold both kinds.  A lane reads and writes nothing of its neighbours: the
+    quadrupeds' q̈ is bit-identical to the one they get in a batch of their own,
+    and so is the chains' under CRBA.  Under ABA a pack of planar chains alone
+    runs the articulated-body passes specialised for planar chains, a pack that
+    also holds a quadruped the general ones: the chains then agree to round-off
+    (FP64: 1e-9 relative to max(|q̈|, 1)) or to the mixed form's bound (2e-5:
+    both within 1e-5 of FP64).  MIXED with the articulated-body algorithm stays
+    within 1e-5 of FP64, MIXED_REFINED within 1e-6, and no status bit is set.
+    A mixed pack once let the FP32 bias forces of its chain lanes overwrite the
+    FP64 bias forces of its contact lanes."""
     if algorithm == "aba" and precision == gpb.MIXED_REFINED:
         pytest.skip("MIXED_REFINED always uses CRBA")
     M3, q3, v3, _ = Model.from_config(3, 75, seed=31)
@@ -178,11 +182,17 @@ def test_mixed_contact_batches(ctx, algorithm, precision):
     st = B.status()
     ref = B.dynamics_continuous(tau, precision=gpb.FP64)
     n3 = int(v3.size)
-    for Mk, qk, vk, sl in ((M3, q3, v3, slice(0, n3)), (M1, q1, v1, slice(n3, None))):
+    chain_tol = 0.0 if algorithm == "crba" else (2e-5 if precision == gpb.MIXED else 1e-9)
+    for Mk, qk, vk, sl, tol in ((M3, q3, v3, slice(0, n3), 0.0), (M1, q1, v1, slice(n3, None), chain_tol)):
         A = Batch(Mk, ctx)
         A.update(qk, vk)
         alone = A.dynamics_continuous(tau[sl], precision=precision)
-        np.testing.assert_array_equal(mix[sl], alone)
+        if tol == 0.0:
+            np.testing.assert_array_equal(mix[sl], alone)
+        else:
+            _, vk_off, _ = Mk.offsets()
+            d = max(rel_err(mix[sl][vk_off[i]:vk_off[i + 1]], alone[vk_off[i]:vk_off[i + 1]]) for i in range(Mk.n))
+            assert d <= tol, d
         A.close()
     # MIXED with CRBA is the FP32 mass-matrix form, limited by cond(H)·ε32: no bound
     bound = {gpb.FP64: 0.0, gpb.MIXED: 1e-5 if algorithm == "aba" else None, gpb.MIXED_REFINED: 1e-6}[precision]

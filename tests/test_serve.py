@@ -53,6 +53,9 @@ def mix_model(seed=3, n=(40, 40, 5, 4)):
 
 CLASSES = [SlotClass(2, 2, 2, packs=1), SlotClass(48, 48, 48, packs=1), SlotClass(1, 7, 6, 8, 1, packs=1),
            SlotClass(13, 19, 18, 4, 1, packs=1)]
+# the same pool with the acrobot and chain classes for planar chains only
+PLANAR_CLASSES = [SlotClass(2, 2, 2, packs=1, planar_only=True), SlotClass(48, 48, 48, packs=1, planar_only=True),
+                  SlotClass(1, 7, 6, 8, 1, packs=1), SlotClass(13, 19, 18, 4, 1, packs=1)]
 
 
 def submit_all(S, M, q0, v0, aux, cfg, horizons, idx):
@@ -76,22 +79,54 @@ def run_server(ctx, M, q0, v0, aux, cfg, horizons, idx, precision, chunk=37, cla
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,algorithm", [(gpb.FP64, gpb.ALGO_CRBA), (gpb.MIXED, gpb.ALGO_CRBA),
-                                                 (gpb.MIXED_REFINED, gpb.ALGO_CRBA), (gpb.FP64, gpb.ALGO_ABA),
-                                                 (gpb.MIXED, gpb.ALGO_ABA)])
-def test_alone_equals_mix_bit_for_bit(ctx, precision, algorithm):
+@pytest.mark.parametrize("precision,algorithm,classes", [
+    (gpb.FP64, gpb.ALGO_CRBA, CLASSES), (gpb.MIXED, gpb.ALGO_CRBA, CLASSES),
+    (gpb.MIXED_REFINED, gpb.ALGO_CRBA, CLASSES), (gpb.FP64, gpb.ALGO_ABA, CLASSES),
+    (gpb.MIXED, gpb.ALGO_ABA, CLASSES), (gpb.FP64, gpb.ALGO_ABA, PLANAR_CLASSES),
+    (gpb.MIXED, gpb.ALGO_ABA, PLANAR_CLASSES)], ids=lambda x: "planar" if x is PLANAR_CLASSES else
+    ("general" if x is CLASSES else None))
+def test_alone_equals_mix_bit_for_bit(ctx, precision, algorithm, classes):
     M, q0, v0, aux, cfg = mix_model()
     rng = np.random.default_rng(5)
     horizons = rng.integers(40, 300, size=M.n)
-    mix = run_server(ctx, M, q0, v0, aux, cfg, horizons, range(M.n), precision, algorithm=algorithm)
+    mix = run_server(ctx, M, q0, v0, aux, cfg, horizons, range(M.n), precision, algorithm=algorithm,
+                     classes=classes)
     # one pack (32 slots) per class: the 40 acrobots and 40 chains queue, and
     # later requests run in slots freed by others (of other sizes for the chains)
     for i in (0, 35, 42, 77, 82, 86, 88):
-        alone = run_server(ctx, M, q0, v0, aux, cfg, horizons, [i], precision, chunk=53, algorithm=algorithm)[i]
+        alone = run_server(ctx, M, q0, v0, aux, cfg, horizons, [i], precision, chunk=53, algorithm=algorithm,
+                           classes=classes)[i]
         qa, va, sa, da, _ = alone
         qm, vm, sm, dm, _ = mix[i]
         assert sa == sm and da == dm == horizons[i]
         assert np.array_equal(qa, qm) and np.array_equal(va, vm), i
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [gpb.FP64, gpb.MIXED])
+def test_planar_classes_match_batch_api(ctx, precision):
+    """Under the articulated-body algorithm a planar chain in a planar-only slot
+    class runs the same specialised passes as a batch of planar chains: its
+    result equals the batch of one bit for bit (acrobots and chains); the other
+    mechanisms run the general passes in both."""
+    M, q0, v0, aux, cfg = mix_model()
+    qo, vo, _ = M.offsets()
+    horizons = np.full(M.n, 120)
+    res = run_server(ctx, M, q0, v0, aux, cfg, horizons, range(M.n), precision, classes=PLANAR_CLASSES,
+                     algorithm=gpb.ALGO_ABA)
+    for i in (1, 38, 45, 78, 81, 87):
+        c = int(cfg[i])
+        B = Batch(M.subset([i]), ctx)
+        B.set_algorithm(gpb.ALGO_ABA)
+        B.update(q0[qo[i]:qo[i + 1]], v0[vo[i]:vo[i + 1]])
+        B.simulate_steps(120, DT[c], 0, precision, control=CONTROL[c],
+                         tau=aux[vo[i]:vo[i + 1]] if c == 3 else None, seed=11 + i, resample_every=10,
+                         sigma=1.0, kp=50.0, kd=2.0)
+        qb, vb = B.state()
+        B.close()
+        qs, vs, st, done, _ = res[i]
+        assert st == 0 and done == 120
+        assert np.array_equal(qb, qs) and np.array_equal(vb, vs), i
 
 
 @pytest.mark.gpu
