@@ -768,6 +768,40 @@ __device__ __forceinline__ void store_svd(const LaneCtx<R>& c, int base, const S
   c.d(base + 5) = s.v.z;
 }
 
+// ---- mechanism kinds with their own instantiation of the passes ------------
+// KIND_GENERAL: any tree.  KIND_PLANAR_CHAIN: revolute joints about ±x/±y/±z
+// with identity joint rotations, each body the child of the previous one, no
+// contacts, colliders or springs.  KIND_FLOATING_TREE: a floating root and
+// revolute joints about ±x/±y/±z below it, identity joint rotations, any tree,
+// point / sphere contacts, no colliders or springs.  Joint type, parent (for a
+// chain), axis kind and the absent cases are then constants: their code drops
+// out of the loops, which shrinks the instruction stream the passes fetch.
+constexpr int KIND_GENERAL = 0, KIND_PLANAR_CHAIN = 1, KIND_FLOATING_TREE = 2;
+template <int KIND>
+__device__ __forceinline__ int kind_type(uint32_t w0, int b) {
+  return KIND == KIND_PLANAR_CHAIN ? 1 : (KIND == KIND_FLOATING_TREE ? (b == 0 ? 3 : 1) : (int)(w0 & 15));
+}
+template <int KIND>
+__device__ __forceinline__ int kind_parent(uint32_t w0, int b) {
+  return KIND == KIND_PLANAR_CHAIN ? b : (int)((w0 >> 4) & 255);
+}
+// flags: a planar chain has no branch bodies; both special kinds have identity
+// joint rotations
+template <int KIND>
+__device__ __forceinline__ uint32_t kind_flags(uint32_t w1) {
+  const uint32_t f = w1 & 255;
+  if (KIND == KIND_PLANAR_CHAIN) return (f & ~(uint32_t)BF_BRANCH) | BF_INIT_ROT_IDENTITY;
+  if (KIND == KIND_FLOATING_TREE) return f | BF_INIT_ROT_IDENTITY;
+  return f;
+}
+// principal axis index of a planar joint, −1 for any other joint
+template <int KIND>
+__device__ __forceinline__ int kind_planar(int type, uint32_t fl, int b) {
+  if (KIND == KIND_PLANAR_CHAIN) return (int)bf_axis_index(fl);
+  if (KIND == KIND_FLOATING_TREE) return b == 0 ? -1 : (int)bf_axis_index(fl);
+  return planar_axis(type, fl);
+}
+
 // Pass 2 of the mixed form: articulated inertias, U, D and the congruence to
 // the parent in double-float, from the FP32 model and the FP32 transforms of
 // pass 1; each body's bias force p = v ×* I v (from its FP32 velocity, plus
@@ -775,7 +809,7 @@ __device__ __forceinline__ void store_svd(const LaneCtx<R>& c, int base, const S
 // recursion in double-float; the bias acceleration c and I^a c in FP32.  A
 // 1-DOF joint's DU record holds FF words (U, 1/D, u); a floating joint's holds
 // the FP64 record of the FP64 form.
-template <typename R, bool PC>
+template <typename R, int KIND>
 __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q, Col<double> v, Col<double> tau,
                                              bool have_tau, bool contacts) {
   using V = V3<R>;
@@ -785,10 +819,8 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
   int ctarget = -1;
   for (int b = c.nb - 1; b >= 0; --b) {
     const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
-    // a planar chain (PC): revolute joints about ±x/±y/±z with identity joint
-    // rotations, each body the child of the previous one, no branches
-    const uint32_t fl = PC ? ((w1 & 255) & ~(uint32_t)BF_BRANCH) : (w1 & 255);
-    const int type = PC ? 1 : (int)(w0 & 15), parent = PC ? b : (int)((w0 >> 4) & 255);
+    const uint32_t fl = kind_flags<KIND>(w1);
+    const int type = kind_type<KIND>(w0, b), parent = kind_parent<KIND>(w0, b);
     const int qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
     const int tb = TOPO_D * b;
     const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
@@ -816,10 +848,10 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
     }
     SVF pa;
     const bool to_parent = parent != 0;
-    const int planar = PC ? (int)bf_axis_index(fl) : planar_axis(type, fl);
+    const int planar = kind_planar<KIND>(type, fl, b);
     if (type == 1 || type == 2) {
       FF Uw[3], Uv[3], D;
-      if (type == 1 && (PC || (fl & BF_AXIS_PRINCIPAL))) {  // a = ±e_k: U = ±(A[:,k], row k of B), D = A_kk
+      if (type == 1 && (KIND != KIND_GENERAL || (fl & BF_AXIS_PRINCIPAL))) {  // a = ±e_k: U = ±(A[:,k], row k of B), D = A_kk
         const int k = (int)bf_axis_index(fl);
         Uw[0] = pick3(k, IA.A[0], IA.A[3], IA.A[4]);
         Uw[1] = pick3(k, IA.A[3], IA.A[1], IA.A[5]);
@@ -851,7 +883,7 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
       }
       // u = τ + τ_spring − Sᵀ p^A (the torque in FP64, split; Sᵀ p^A in double-float)
       double tt = have_tau ? tau[vo] : 0.0;
-      if (!PC && type == 2 && (w1 & BF_SPRING) && c.springs)
+      if (KIND == KIND_GENERAL && type == 2 && (w1 & BF_SPRING) && c.springs)
         tt += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
       const FF sp = type == 1 ? ff_dot3f(pA.w[0], pA.w[1], pA.w[2], ax.x, ax.y, ax.z)
                               : ff_dot3f(pA.v[0], pA.v[1], pA.v[2], ax.x, ax.y, ax.z);
@@ -967,13 +999,15 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
 
 // One dynamics evaluation by the articulated-body algorithm.  q̈ into qdd;
 // GPB status bits (CHOL_FAIL for a non-positive articulated inertia D).
-template <typename R, bool PC>
+template <typename R, int KIND>
 __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<double> v, Col<double> tau,
                                      bool have_tau, Col<double> qdd, Col<double> cf, bool want_cf) {
   const LaneCtx<R> c = cin;  // private copy: stores through scratch pointers cannot alias it
   using V = V3<R>;
   using VD = V3<double>;
-  const bool contacts = !PC && (c.nc > 0 || c.nu > 1);  // world poses in FP64 (points or cuboid pairs)
+  // world poses in FP64 (points or cuboid pairs)
+  const bool contacts = KIND == KIND_PLANAR_CHAIN ? false
+                        : (KIND == KIND_FLOATING_TREE ? c.nc > 0 : (c.nc > 0 || c.nu > 1));
   const bool wide = contacts || sizeof(R) == 8;  // FP64 joint transforms
   const V zero{R(0), R(0), R(0)};
   V pw_ = zero, pv_ = zero;                  // parent velocity (chain carry)
@@ -989,9 +1023,9 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
   // ---- pass 1 (outward): transforms, velocities, bias terms, contacts ------
   for (int b = 0; b < c.nb; ++b) {
     const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
-    const int type = PC ? 1 : (int)(w0 & 15), parent = PC ? b : (int)((w0 >> 4) & 255);
+    const int type = kind_type<KIND>(w0, b), parent = kind_parent<KIND>(w0, b);
     const int qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
-    const uint32_t fl = PC ? (((w1 & 255) & ~(uint32_t)BF_BRANCH) | BF_INIT_ROT_IDENTITY) : (w1 & 255);
+    const uint32_t fl = kind_flags<KIND>(w1);
     V om = zero, vl = zero;
     VD omd{0.0, 0.0, 0.0}, vld{0.0, 0.0, 0.0};
     VD posw{0.0, 0.0, 0.0};
@@ -1020,7 +1054,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     // child → parent transform (Rr, t): FP64 record Rd / td; Rr, t in R
     const int tb = TOPO_D * b;
     const bool rid = (fl & BF_INIT_ROT_IDENTITY) != 0;
-    const bool planar = PC || (type == 1 && rid && (fl & BF_AXIS_PRINCIPAL));
+    const bool planar = kind_planar<KIND>(type, fl, b) >= 0 && rid;
     M3<double> Rd = eye3<double>();
     VD td{c.td(tb + TD_TINIT), c.td(tb + TD_TINIT + 1), c.td(tb + TD_TINIT + 2)};
     M3<R> Rr;
@@ -1286,7 +1320,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     pR = Rw;
   }
   // ---- cuboid pairs: p −= W (body frame, FP64 records of contact mechanisms)
-  if (!PC && c.nu > 1) {
+  if (KIND == KIND_GENERAL && c.nu > 1) {
     st |= lane_cuboid_pairs(c);
     for (int b = 0; b < c.nb; ++b) {
       const int uslot = (int)((c.w(2 * b + 1) >> W1_CUBOID_SHIFT) & 15u);
@@ -1297,15 +1331,15 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
   // A child that is the next body (every link of a chain) hands its terms to
   // the parent in registers; other children accumulate into the parent's slot.
   if constexpr (sizeof(R) == 4) {
-    st |= aba_inward_ff<R, PC>(c, q, v, tau, have_tau, contacts);
+    st |= aba_inward_ff<R, KIND>(c, q, v, tau, have_tau, contacts);
   } else {
     ABI carryI{};
     SV<R> carryP{zero, zero};
     int ctarget = -1;
     for (int b = c.nb - 1; b >= 0; --b) {
       const uint32_t w0 = c.w(2 * b), w1 = c.w(2 * b + 1);
-      const uint32_t fl = PC ? ((w1 & 255) & ~(uint32_t)BF_BRANCH) : (w1 & 255);
-      const int type = PC ? 1 : (int)(w0 & 15), parent = PC ? b : (int)((w0 >> 4) & 255);
+      const uint32_t fl = kind_flags<KIND>(w1);
+      const int type = kind_type<KIND>(w0, b), parent = kind_parent<KIND>(w0, b);
       const int qo = (w0 >> 12) & 1023, vo = (w0 >> 22) & 1023;
       const int tb = TOPO_D * b;
       ABI IA = body_abi(c, tb);
@@ -1326,7 +1360,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       const bool to_parent = parent != 0;
       if (type == 1 || type == 2) {
         double Uw[3], Uv[3], D;
-        if (type == 1 && (PC || (fl & BF_AXIS_PRINCIPAL))) {  // a = ±e_k: U = ±(A[:,k], row k of B), D = A_kk
+        if (type == 1 && (KIND != KIND_GENERAL || (fl & BF_AXIS_PRINCIPAL))) {  // a = ±e_k: U = ±(A[:,k], row k of B), D = A_kk
           const int k = (int)bf_axis_index(fl);
           Uw[0] = pick3(k, IA.A[0], IA.A[3], IA.A[4]);
           Uw[1] = pick3(k, IA.A[3], IA.A[1], IA.A[5]);
@@ -1362,7 +1396,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         // u = τ + τ_spring − Sᵀ p^A
         const V axr{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
         double u = have_tau ? tau[vo] : 0.0;
-        if (!PC && type == 2 && (w1 & BF_SPRING) && c.springs)
+        if (KIND == KIND_GENERAL && type == 2 && (w1 & BF_SPRING) && c.springs)
           u += -c.td(tb + TD_SPRING) * (q[qo] - c.td(tb + TD_SPRING + 1));
         if (contacts) {
           const VD axd{c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
@@ -1429,7 +1463,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         if (type != 3) {
           double Rr[9];
           const VD t{c.d(c.L.I + 12 * b + 9), c.d(c.L.I + 12 * b + 10), c.d(c.L.I + 12 * b + 11)};
-          const int planar = PC ? (int)bf_axis_index(fl) : planar_axis(type, fl);
+          const int planar = kind_planar<KIND>(type, fl, b);
           double co = 1.0, si = 0.0;
           if (planar >= 0) {  // (cos, sin) record; abi_to_parent does not read Rr then
             co = c.d(c.L.I + 12 * b);
@@ -1455,7 +1489,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         // force to the parent frame: (Rr n + t × Rr f, Rr f)
         M3<R> RrR;
         V tr;
-        load_xf(c, b, PC ? (int)bf_axis_index(fl) : planar_axis(type, fl), RrR, tr);
+        load_xf(c, b, kind_planar<KIND>(type, fl, b), RrR, tr);
         const SV<R> fp = force_to_parent(RrR, tr, pa);
         if (pb == b - 1) {
           carryP = fp;
@@ -1478,8 +1512,8 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
   SV<R> ap_{zero, zero};
   for (int b = 0; b < c.nb; ++b) {
     const uint32_t w0 = c.w(2 * b);
-    const uint32_t w1 = PC ? (c.w(2 * b + 1) & ~(uint32_t)BF_BRANCH) : c.w(2 * b + 1);
-    const int type = PC ? 1 : (int)(w0 & 15), parent = PC ? b : (int)((w0 >> 4) & 255);
+    const uint32_t w1 = (c.w(2 * b + 1) & ~(uint32_t)255) | kind_flags<KIND>(c.w(2 * b + 1));
+    const int type = kind_type<KIND>(w0, b), parent = kind_parent<KIND>(w0, b);
     const int vo = (w0 >> 22) & 1023;
     const int tb = TOPO_D * b;
     SV<R> a;
@@ -1492,7 +1526,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     }
     M3<R> Rr;
     V t;
-    load_xf(c, b, PC ? (int)bf_axis_index(w1 & 255) : planar_axis(type, w1 & 255), Rr, t);
+    load_xf(c, b, kind_planar<KIND>(type, w1 & 255, b), Rr, t);
     const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
     // a' = X a_p + c (the mixed form forms c again from the body velocity,
     // which a branch body's acceleration overwrites only below)

@@ -97,7 +97,7 @@ int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
     return fail(GPB_E_RANGE, "instance " + std::to_string(i) + ": body count outside [0, 64]");
   I.nq = I.nv = 0;
   I.chain = true;
-  I.planar = true;
+  bool planar_chain = true, floating_tree = I.nb > 0;
   uint64_t sig = 1469598103934665603ull;
   for (int b = 0; b < I.nb; ++b) {
     int t = m->joint_type[I.j0 + b], p = m->joint_parent[I.j0 + b];
@@ -109,14 +109,15 @@ int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
       return fail(GPB_E_INVAL, "instance " + std::to_string(i) + ": joint " + std::to_string(b + 1) +
                                    " has parent " + std::to_string(p) + " (must be < its own number)");
     if (p != b) I.chain = false;
-    {
+    {  // the kinds with their own instantiation of the articulated-body passes
       const double* iso = m->joint_iso + 7 * (size_t)(I.j0 + b);
       const double* ax = m->joint_axis + 3 * (size_t)(I.j0 + b);
       const int nz = (ax[0] != 0.0) + (ax[1] != 0.0) + (ax[2] != 0.0);
       const double amax = std::max(std::fabs(ax[0]), std::max(std::fabs(ax[1]), std::fabs(ax[2])));
-      if (t != GPB_JOINT_REVOLUTE || p != b || !(iso[0] == 0.0 && iso[1] == 0.0 && iso[2] == 0.0 && iso[3] == 1.0) ||
-          nz != 1 || amax != 1.0)
-        I.planar = false;
+      const bool ident = iso[0] == 0.0 && iso[1] == 0.0 && iso[2] == 0.0 && iso[3] == 1.0;
+      const bool principal_revolute = t == GPB_JOINT_REVOLUTE && nz == 1 && amax == 1.0 && ident;
+      if (!principal_revolute || p != b) planar_chain = false;
+      if (b == 0 ? !(t == GPB_JOINT_FLOATING && p == 0 && ident) : !principal_revolute) floating_tree = false;
     }
     I.nq += joint_nq(t);
     I.nv += joint_nv(t);
@@ -150,7 +151,11 @@ int gpb::inspect_instance(const gpb_model* m, int64_t i, InstInfo* out) {
                                    std::to_string(GPB_MAX_CUBOIDS) + " cuboid colliders");
   }
   I.mvs = I.nc * I.nh + I.nu * (I.nu - 1) / 2;
-  if (I.nc > 0 || I.nu > 0) I.planar = false;
+  bool springs = false;
+  for (int b = 0; b < I.nb && m->joint_spring; ++b) springs = springs || m->joint_spring[2 * (size_t)(I.j0 + b)] != 0.0;
+  if (I.nc > 0 || I.nu > 0 || springs) planar_chain = false;
+  if (I.nu > 0 || springs) floating_tree = false;
+  I.kind = planar_chain ? 1 : (floating_tree ? 2 : 0);
   sig = (sig ^ (uint64_t)(I.nc * 7 + I.nh + 1000 * I.nu)) * 1099511628211ull;
   I.sig = sig;
   return GPB_OK;
@@ -201,7 +206,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
     std::memset(&P, 0, sizeof(P));
     P.count = (int32_t)std::min<int64_t>(LANES, n - p * LANES);
     P.chain = 1;
-    P.planar = 1;
+    P.kind = -1;
     P.minnv = GPB_MAX_DOF;
     for (int l = 0; l < P.count; ++l) {
       const InstInfo& I = info[order[p * LANES + l]];
@@ -214,7 +219,7 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
       P.mvs = std::max(P.mvs, I.mvs);
       P.minnv = std::min(P.minnv, I.nv);
       if (!I.chain) P.chain = 0;
-      if (!I.planar) P.planar = 0;
+      P.kind = (P.kind < 0 || P.kind == I.kind) ? I.kind : 0;
     }
     P.topo = rt;
     P.ctc = rc;
@@ -233,6 +238,15 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
     rl += LANE_I;
     rs += scratch_layout(P.nb, P.nq, P.nv, P.nc, P.nu).total;
   }
+  // A special kind only for a batch of that kind alone: when its packs run
+  // beside packs of other kinds, the instantiations share each SM's instruction
+  // cache and the batch runs slower than with the general one (16,384
+  // quadrupeds + 16,384 chains, mixed: 40.8 against 47.4 M instance-steps/s on
+  // GB300 with the chains' packs specialised).
+  int kind = npacks > 0 ? std::max(B->packs_h[0].kind, 0) : 0;
+  for (const PackDesc& P : B->packs_h)
+    if (P.kind != kind) kind = 0;
+  for (PackDesc& P : B->packs_h) P.kind = kind;
   const size_t L = LANES;
   std::vector<uint32_t> W(rt * 2 * L, 0);
   std::vector<double> TD(rt * TOPO_D * L, 0.0), CD(rc * CTC_D * L, 0.0), HD(rh * HS_D * L, 0.0);

@@ -57,7 +57,7 @@ struct InstInfo {
   int32_t j0, nb, nq, nv, c0, nc, h0, nh, model, nu;
   int32_t mvs;  // velocity stepping: potential contacts (points × half-spaces + cuboid pairs)
   bool chain;
-  bool planar;   // a planar chain (PackDesc::planar)
+  int32_t kind;  // 0 general, 1 planar chain, 2 floating tree (PackDesc::kind)
   uint64_t sig;  // topology class
 };
 

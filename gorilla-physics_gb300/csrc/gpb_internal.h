@@ -49,10 +49,9 @@ struct PackDesc {
   int32_t nu;   // largest cuboid-collider count of its lanes
   int32_t mvs;  // velocity stepping: largest potential contact count of its lanes
                 // (points × half-spaces + cuboid pairs), 0 = none
-  int32_t planar;  // 1: every lane is a planar chain — revolute joints about ±x/±y/±z with
-                   // identity joint rotations, each body the child of the previous one, no
-                   // contacts, colliders or springs (the articulated-body passes drop the
-                   // other cases at compile time)
+  int32_t kind;  // mechanism kind of every lane, for the instantiation of the
+                 // articulated-body passes (0 general, 1 planar chain, 2 floating tree;
+                 // see gpb_aba.cuh); general unless every pack of the batch has one kind
   // bases in rows (one row = LANES elements)
   int64_t topo;   // topology bodies (2 int words / TOPO_D reals per body)
   int64_t ctc;    // contacts

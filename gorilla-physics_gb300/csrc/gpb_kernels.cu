@@ -68,7 +68,7 @@ struct RealTopo<float> {
 template <typename R>
 struct LaneCtx {
   int lane, nb, nq, nv, nc, nh, model, chain;
-  int planar;   // every lane of the pack is a planar chain (PackDesc::planar)
+  int kind;     // mechanism kind shared by every lane of the pack (PackDesc::kind)
   int nu;       // cuboid colliders (slots 1..nu in body order)
   int springs;  // prismatic springs act (off for Articulated::free_velocity)
   int allx;     // keep every body's world pose in X (velocity stepping)
@@ -960,9 +960,11 @@ struct EvalFP64 {
   int algo;  // GPB_ALGO_CRBA / GPB_ALGO_ABA
   __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
                             Col<double> cf = Col<double>{nullptr}, bool want_cf = false) const {
-    if (algo == 1)
-      return c.planar ? lane_aba<double, true>(c, q, v, t, ht, x, cf, want_cf)
-                      : lane_aba<double, false>(c, q, v, t, ht, x, cf, want_cf);
+    if (algo == 1) {
+      if (c.kind == KIND_PLANAR_CHAIN) return lane_aba<double, KIND_PLANAR_CHAIN>(c, q, v, t, ht, x, cf, want_cf);
+      if (c.kind == KIND_FLOATING_TREE) return lane_aba<double, KIND_FLOATING_TREE>(c, q, v, t, ht, x, cf, want_cf);
+      return lane_aba<double, KIND_GENERAL>(c, q, v, t, ht, x, cf, want_cf);
+    }
     return lane_dynamics<double, double>(c, q, v, t, ht, x, cf, want_cf);
   }
 };
@@ -971,9 +973,11 @@ struct EvalMixed {  // CRBA: FP32 sweeps and fill, FP64 Cholesky when n > 12; AB
   int algo;
   __device__ int operator()(Col<double> q, Col<double> v, Col<double> t, bool ht, Col<double> x,
                             Col<double> cf = Col<double>{nullptr}, bool want_cf = false) const {
-    if (algo == 1)
-      return c.planar ? lane_aba<float, true>(c, q, v, t, ht, x, cf, want_cf)
-                      : lane_aba<float, false>(c, q, v, t, ht, x, cf, want_cf);
+    if (algo == 1) {
+      if (c.kind == KIND_PLANAR_CHAIN) return lane_aba<float, KIND_PLANAR_CHAIN>(c, q, v, t, ht, x, cf, want_cf);
+      if (c.kind == KIND_FLOATING_TREE) return lane_aba<float, KIND_FLOATING_TREE>(c, q, v, t, ht, x, cf, want_cf);
+      return lane_aba<float, KIND_GENERAL>(c, q, v, t, ht, x, cf, want_cf);
+    }
     if (c.nv <= 12) return lane_dynamics<float, float>(c, q, v, t, ht, x, cf, want_cf);
     return lane_dynamics<float, double>(c, q, v, t, ht, x, cf, want_cf);
   }
@@ -1060,7 +1064,7 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   c.model = li[6 * LANES];
   c.nu = b.plain ? 0 : li[7 * LANES];  // free_velocity: no colliders
   c.chain = pd.chain;
-  c.planar = pd.planar;
+  c.kind = pd.kind;
   c.springs = b.plain ? 0 : 1;
   c.allx = 0;
   c.grav = b.gravity;

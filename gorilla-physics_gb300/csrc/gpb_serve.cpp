@@ -253,7 +253,7 @@ extern "C" int gpb_server_create(gpb_ctx* ctx, const gpb_server_opts* o, gpb_ser
       P.nh = C.caps.max_halfspaces;
       P.nu = C.caps.max_cuboids;
       P.chain = 0;
-      P.planar = C.caps.planar_only ? 1 : 0;
+      P.kind = C.caps.planar_only ? 1 : 0;
       P.topo = rt;
       P.ctc = rc;
       P.hs = rh;
@@ -393,7 +393,7 @@ extern "C" int gpb_server_submit(gpb_server* S, const gpb_model* m, int64_t firs
     // smallest class that fits; a planar chain takes a planar-only class first.
     // The choice depends on the request alone, so its path (and its bits) do too.
     int best = -1;
-    for (int pass = R.info.planar ? 0 : 1; pass < 2 && best < 0; ++pass) {
+    for (int pass = R.info.kind == 1 ? 0 : 1; pass < 2 && best < 0; ++pass) {
       for (int c = 0; c < (int)S->classes.size(); ++c) {
         const gpb_slot_class& cap = S->classes[c].caps;
         if ((cap.planar_only != 0) != (pass == 0)) continue;
