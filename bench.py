@@ -372,10 +372,11 @@ def run_gpu(args):
         # launch shape for this workload and form (short trials, state restored)
         if args.warps_per_sm:
             B.set_launch(args.warps_per_sm)
-            w, c = args.warps_per_sm, 0
+            B.set_mapping(1)
+            w, c, lanes = args.warps_per_sm, 0, 1
         else:
-            w, c = B.autotune(dt, 0, prec, trial_steps=10, **kw)
-        launch[name] = {"warps_per_sm": w, "coop_min_dof": c}
+            w, c, lanes = B.autotune(dt, 0, prec, trial_steps=10, **kw)
+        launch[name] = {"warps_per_sm": w, "coop_min_dof": c, "lanes_per_instance": lanes}
         if args.warmup:
             B.simulate_steps(args.warmup, dt, 0, prec, step0=0, **kw)
         barrier()
@@ -888,7 +889,7 @@ def run_cuboids(args):
         B.set_algorithm(algo)
         B.update(q0, v0)
         B.clear_status()
-        w, _ = B.autotune(CUBOID_DT, 0, prec, trial_steps=10)
+        w, _, _ = B.autotune(CUBOID_DT, 0, prec, trial_steps=10)
         if args.warmup:
             B.simulate_steps(args.warmup, CUBOID_DT, 0, prec)
         if world > 1:
@@ -1057,7 +1058,7 @@ def run_vstep(args):
     M, q0, v0 = resting_cubes(n, shard_seed(args.seed, rank))
     B = Batch(M, ctx)
     B.update(q0, v0)
-    w, _ = B.autotune(VSTEP_DT, gpb.VELOCITY_STEPPING, gpb.FP64, trial_steps=5)
+    w, _, _ = B.autotune(VSTEP_DT, gpb.VELOCITY_STEPPING, gpb.FP64, trial_steps=5)
     if args.warmup:
         B.simulate_steps(args.warmup, VSTEP_DT, gpb.VELOCITY_STEPPING)
     ctx.synchronize()

@@ -888,7 +888,7 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
       const FF sp = type == 1 ? ff_dot3f(pA.w[0], pA.w[1], pA.w[2], ax.x, ax.y, ax.z)
                               : ff_dot3f(pA.v[0], pA.v[1], pA.v[2], ax.x, ax.y, ax.z);
       const FF uf = ff_sub(ff_from_double(tt), sp);
-      if (type == 1) {  // revolute armature (src/hybrid/articulated/mod.rs:244-247)
+      if (type == 1 && c.armature) {  // free_velocity: revolute armature (src/hybrid/articulated/mod.rs:244-247)
         const float arm = c.t(tb + TD_ARMATURE);
         if (arm != 0.0f) D = ff_add(D, ff(arm));
       }
@@ -1404,7 +1404,8 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
         } else {
           u -= double(type == 1 ? dot(axr, pA.w) : dot(axr, pA.v));
         }
-        if (type == 1) D += c.td(tb + TD_ARMATURE);  // revolute armature (src/hybrid/articulated/mod.rs:244-247)
+        if (type == 1 && c.armature)  // free_velocity: revolute armature (src/hybrid/articulated/mod.rs:244-247)
+          D += c.td(tb + TD_ARMATURE);
         if (!(D > 0.0)) st |= 2;  // GPB_ST_CHOL_FAIL
         const double Dinv = 1.0 / D;
         const int du = c.L.DU + DU_D * vo;

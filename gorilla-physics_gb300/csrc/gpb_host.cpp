@@ -187,6 +187,18 @@ extern "C" int gpb_batch_create(gpb_ctx* ctx, const gpb_model* m, gpb_batch** ou
   B->nv_total = B->v_off[n];
   B->nc_total = B->c_off[n];
 
+  // the body-parallel mapping (serial chains of revolute, prismatic and fixed
+  // joints, no cuboid colliders)
+  B->group_ok = n > 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const InstInfo& I = info[i];
+    B->nb_max = std::max(B->nb_max, (int)I.nb);
+    B->nv_max = std::max(B->nv_max, (int)I.nv);
+    bool ok = I.chain && I.nu == 0;
+    for (int b = 0; b < I.nb && ok; ++b) ok = m->joint_type[I.j0 + b] != GPB_JOINT_FLOATING;
+    B->group_ok = B->group_ok && ok;
+  }
+
   // sort: largest work first (the persistent queue then balances), same topology together
   std::vector<int64_t> order(n);
   std::iota(order.begin(), order.end(), 0);
@@ -407,6 +419,28 @@ static int32_t coop_packs(const gpb_batch* b, int precision) {
   return n;
 }
 
+// Bodies per lane of the body-parallel mapping with `lanes` lanes per
+// instance, 0 if the batch cannot run it that way.
+static int group_bodies_per_lane(const gpb_batch* b, int lanes) {
+  if (!b->group_ok || lanes < 2 || lanes > LANES || (lanes & (lanes - 1))) return 0;
+  const int s = (b->nb_max + lanes - 1) / lanes;
+  return s <= 1 ? 1 : (s == 2 ? 2 : 0);
+}
+
+extern "C" int gpb_batch_set_mapping(gpb_batch* b, int lanes_per_instance) {
+  if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_mapping: batch is NULL");
+  if (lanes_per_instance != 1 && !group_bodies_per_lane(b, lanes_per_instance)) {
+    if (!b->group_ok)
+      return fail(GPB_E_INVAL, "gpb_batch_set_mapping: several lanes per instance need a batch of serial chains "
+                               "of revolute, prismatic and fixed joints without cuboid colliders");
+    return fail(GPB_E_INVAL, "gpb_batch_set_mapping: lanes_per_instance must be 1 or a power of two in [2, 32] "
+                             "with at most two bodies per lane (this batch has chains of " +
+                                 std::to_string(b->nb_max) + " bodies)");
+  }
+  b->lanes = lanes_per_instance;
+  return GPB_OK;
+}
+
 extern "C" int gpb_batch_set_launch(gpb_batch* b, int warps_per_sm) {
   if (!b) return fail(GPB_E_INVAL, "gpb_batch_set_launch: batch is NULL");
   if (warps_per_sm < 0 || warps_per_sm > 64 || warps_per_sm % 4 != 0)
@@ -573,10 +607,20 @@ static int run_simulate(gpb_batch* b, double dt, int64_t K, int64_t step0, int i
     p.history = b->hist.p;
     p.record_every = record_every;
   }
-  p.ncoop = coop_packs(b, precision);
+  // body-parallel mapping: GPB_FP64 steps of a chain batch, when chosen
+  const int gs = precision == GPB_FP64 && b->algorithm == GPB_ALGO_CRBA && integrator != GPB_VELOCITY_STEPPING &&
+                         b->lanes > 1
+                     ? group_bodies_per_lane(b, b->lanes)
+                     : 0;
+  p.ncoop = gs ? 0 : coop_packs(b, precision);
+  p.group = gs ? b->lanes : 0;
+  p.group_nvp = b->nv_max;
   if (b->npacks > 0 && K > 0) {
     CUDA_TRY(cudaEventRecord(b->ctx->ev0, s));
-    CUDA_TRY(launch_simulate(b->dev(), p, b->ctx->num_sms, b->warps_per_sm, s));
+    if (gs)
+      CUDA_TRY(launch_simulate_group(b->dev(), p, gs, b->ctx->num_sms, s));
+    else
+      CUDA_TRY(launch_simulate(b->dev(), p, b->ctx->num_sms, b->warps_per_sm, s));
     CUDA_TRY(cudaEventRecord(b->ctx->ev1, s));
     b->ctx->timed = true;
     b->ctx->launches++;
@@ -603,7 +647,7 @@ extern "C" int gpb_step(gpb_batch* b, double dt, const double* tau, int integrat
 // current state (restored after every trial and at the end).
 extern "C" int gpb_batch_autotune(gpb_batch* b, double dt, int integrator, int precision,
                                   const gpb_control_params* control, int trial_steps, int* warps_per_sm,
-                                  int* coop_min_dof) {
+                                  int* coop_min_dof, int* lanes_per_instance) {
   if (!b) return fail(GPB_E_INVAL, "gpb_batch_autotune: batch is NULL");
   if (int r = check_enums(integrator, precision)) return r;
   if (trial_steps < 1) return fail(GPB_E_INVAL, "gpb_batch_autotune: trial_steps must be >= 1");
@@ -628,24 +672,32 @@ extern "C" int gpb_batch_autotune(gpb_batch* b, double dt, int integrator, int p
     return e;
   };
   CUDA_TRY(save_restore(true));
-  const int keep_w = b->warps_per_sm, keep_c = b->coop_min_dof;
-  // 4 warps per SM and every further multiple of 4 the kernel's registers
-  // leave room for, up to 16
+  const int keep_w = b->warps_per_sm, keep_c = b->coop_min_dof, keep_l = b->lanes;
+  struct Shape {
+    int w, c, l;  // warps per SM, block-cooperative threshold, lanes per instance
+  };
+  // one lane per instance: 4 warps per SM and every further multiple of 4 the
+  // kernel's registers leave room for, up to 16
   int wmax = 8;
   CUDA_TRY(simulate_max_warps_per_sm(precision, &wmax));
-  std::vector<std::pair<int, int>> cand;
+  std::vector<Shape> cand;
   for (int w = 4; w <= 16 && (w == 4 || w <= wmax); w += 4) {
-    cand.push_back({w, 0});
+    cand.push_back({w, 0, 1});
     if (precision != GPB_MIXED_REFINED && b->algorithm == GPB_ALGO_CRBA && b->npacks > 0 &&
         b->packs_h[0].minnv >= 32)
-      for (int c : {40, 32}) cand.push_back({w, c});
+      for (int c : {40, 32}) cand.push_back({w, c, 1});
   }
+  // body-parallel chains (the CRBA route): the group sizes with one or two bodies per lane
+  if (precision == GPB_FP64 && b->algorithm == GPB_ALGO_CRBA && integrator != GPB_VELOCITY_STEPPING)
+    for (int l = 2; l <= LANES; l *= 2)
+      if (group_bodies_per_lane(b, l) && (l < 2 * b->nb_max || l == 2)) cand.push_back({0, 0, l});
   double best = 1e300;
-  std::pair<int, int> pick{keep_w, keep_c};
+  Shape pick{keep_w, keep_c, keep_l};
   int err = GPB_OK;
   for (const auto& cw : cand) {
-    b->warps_per_sm = cw.first;
-    b->coop_min_dof = cw.second;
+    b->warps_per_sm = cw.w;
+    b->coop_min_dof = cw.c;
+    b->lanes = cw.l;
     CUDA_TRY(save_restore(false));
     // one untimed step, then the timed trial
     err = run_simulate(b, dt, 1, 0, integrator, precision, control, 0, nullptr);
@@ -657,13 +709,15 @@ extern "C" int gpb_batch_autotune(gpb_batch* b, double dt, int integrator, int p
       pick = cw;
     }
   }
-  b->warps_per_sm = err == GPB_OK ? pick.first : keep_w;
-  b->coop_min_dof = err == GPB_OK ? pick.second : keep_c;
+  b->warps_per_sm = err == GPB_OK ? pick.w : keep_w;
+  b->coop_min_dof = err == GPB_OK ? pick.c : keep_c;
+  b->lanes = err == GPB_OK ? pick.l : keep_l;
   CUDA_TRY(save_restore(false));
   CUDA_TRY(cudaStreamSynchronize(s));
   if (err != GPB_OK) return err;
-  if (warps_per_sm) *warps_per_sm = pick.first;
-  if (coop_min_dof) *coop_min_dof = pick.second;
+  if (warps_per_sm) *warps_per_sm = pick.w;
+  if (coop_min_dof) *coop_min_dof = pick.c;
+  if (lanes_per_instance) *lanes_per_instance = pick.l;
   return GPB_OK;
 }
 

@@ -208,6 +208,9 @@ struct gpb_batch {
   int32_t npacks = 0;
   int warps_per_sm = 0;  // resident warps per SM of the step kernel (0 = occupancy limit)
   int coop_min_dof = -1; // block-cooperative packs: DOF threshold (-1 = default, 0 = off)
+  int lanes = 1;         // lanes per instance of GPB_FP64 steps (1, or 2..32: body-parallel chains)
+  bool group_ok = false; // every instance is a serial chain of 1-DOF or fixed joints without colliders
+  int nb_max = 0, nv_max = 0;
   int algorithm = GPB_ALGO_CRBA;
   double gravity = 9.81;  // src/lib.rs:39
   std::vector<int64_t> q_off, v_off, c_off;  // user layout, [n+1]

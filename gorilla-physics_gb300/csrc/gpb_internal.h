@@ -233,6 +233,8 @@ struct StepParams {
   int32_t ncoop;        // packs [0, ncoop) are stepped by a whole 4-warp block
   int32_t free_velocity;  // dynamics-only: write v + vfree_dt·q̈ (no contacts, no springs)
   double vfree_dt;
+  int32_t group;        // body-parallel mapping: lanes per instance (launch_simulate_group)
+  int32_t group_nvp;    // body-parallel mapping: largest DOF count of the batch
 };
 
 // Launchers (gpb_kernels.cu).  All return a cudaError_t.
@@ -240,6 +242,11 @@ struct StepParams {
 // occupancy limit; otherwise rounded to whole 4-warp blocks and capped by it).
 cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p,
                             int num_sms, int warps_per_sm, cudaStream_t s);
+// Body-parallel mapping of serial chains (gpb_group.cuh): p.group lanes per
+// instance, bodies_per_lane = 1 or 2 (p.group · bodies_per_lane ≥ every
+// instance's body count), FP64.
+cudaError_t launch_simulate_group(const DeviceBatch& b, const StepParams& p, int bodies_per_lane, int num_sms,
+                                  cudaStream_t s);
 cudaError_t launch_dynamics(const DeviceBatch& b, const StepParams& p, cudaStream_t s);
 // Resident warps per SM the step kernel of `precision` can hold (registers).
 cudaError_t simulate_max_warps_per_sm(int precision, int* warps);

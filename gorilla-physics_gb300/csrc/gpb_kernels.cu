@@ -71,6 +71,8 @@ struct LaneCtx {
   int kind;     // mechanism kind shared by every lane of the pack (PackDesc::kind)
   int nu;       // cuboid colliders (slots 1..nu in body order)
   int springs;  // prismatic springs act (off for Articulated::free_velocity)
+  int armature; // revolute armature adds to M's diagonal: Articulated::free_velocity only
+                // (src/hybrid/articulated/mod.rs:244-247; dynamics.rs's mass matrix has none)
   int allx;     // keep every body's world pose in X (velocity stepping)
   double grav;  // gravitational acceleration along −z
   const uint32_t* W;  // topology words (row base applied, lane applied)
@@ -825,8 +827,9 @@ __device__ __noinline__ void lane_fill(const LaneCtx<R>& cin, int w, int nw) {
     const int nvb = type == 3 ? 6 : (type == 0 ? 0 : 1);
     if (nvb == 0) continue;
     const SI<R> Ic = load_si(c, c.L.I + 10 * b);
-    // a revolute joint's armature adds to its diagonal (src/hybrid/articulated/mod.rs:244-247)
-    const R arm = type == 1 ? c.t(TOPO_D * b + TD_ARMATURE) : R(0);
+    // a revolute joint's armature adds to its diagonal in free_velocity
+    // (src/hybrid/articulated/mod.rs:244-247)
+    const R arm = type == 1 && c.armature ? c.t(TOPO_D * b + TD_ARMATURE) : R(0);
     for (int k = 0; k < nvb; ++k) {
       const int row = vo + k;
       if ((row >> 2) % nw != w) continue;
@@ -1066,6 +1069,7 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   c.chain = pd.chain;
   c.kind = pd.kind;
   c.springs = b.plain ? 0 : 1;
+  c.armature = b.plain ? 1 : 0;
   c.allx = 0;
   c.grav = b.gravity;
   c.W = b.topoW + pd.topo * 2 * LANES + lane;
@@ -1131,6 +1135,7 @@ struct EvalOf<2> {
 };
 
 #include "gpb_coop.cuh"
+#include "gpb_group.cuh"
 
 // The mixed form at three blocks per SM (168 registers per thread): the
 // compiler's own allocation for it otherwise grows to 255 with the FP64
@@ -1371,6 +1376,31 @@ cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int num_s
   if (grid > want) grid = want;
   if (grid < 1) grid = 1;
   kern<<<(unsigned)grid, threads, 0, s>>>(b, p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_simulate_group(const DeviceBatch& b, const StepParams& p, int bodies_per_lane, int num_sms,
+                                  cudaStream_t s) {
+  if (p.group < 2 || p.group > LANES || (p.group & (p.group - 1)) || bodies_per_lane < 1 || bodies_per_lane > 2 ||
+      p.group_nvp < 0 || p.group_nvp > 2 * p.group)
+    return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(b.queue, 0, 2 * sizeof(int32_t), s);
+  if (e != cudaSuccess) return e;
+  const int threads = 128;
+  const size_t smem = (size_t)(threads / 32) * (LANES / p.group) * grp::smem_words(p.group_nvp) * sizeof(double);
+  auto kern = bodies_per_lane == 1 ? group_kernel<1> : group_kernel<2>;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int64_t items = (int64_t)(b.active ? b.nactive : b.npacks) * p.group;
+  int64_t grid = (int64_t)num_sms * per_sm;
+  const int64_t want = (items + (threads / 32) - 1) / (threads / 32);
+  if (grid > want) grid = want;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, threads, smem, s>>>(b, p);
   return cudaGetLastError();
 }
 

@@ -297,7 +297,8 @@ __device__ __noinline__ int lane_link(const LaneCtx<R>& cin, Col<double> q, Col<
       if (type == 2 && (w1 & BF_SPRING) && c.springs) {  // src/dynamics.rs:298-315
         r += -double(c.t(tb + TD_SPRING)) * (q[qo] - double(c.t(tb + TD_SPRING + 1)));
       }
-      const double arm = type == 1 ? double(c.t(tb + TD_ARMATURE)) : 0.0;  // revolute armature
+      // free_velocity: revolute armature (src/hybrid/articulated/mod.rs:244-247)
+      const double arm = type == 1 && c.armature ? double(c.t(tb + TD_ARMATURE)) : 0.0;
       if (RESIDUAL) {  // difference of nearly equal terms: form it in FP64
         c.template x<RC>(c.L.rhs + vo + k) = RC(r - double(s_dot<R>(type, ax, k, f)) - arm * xacc[vo + k]);
         continue;

@@ -134,7 +134,8 @@ SIGNATURES = [
     ("gpb_batch_set_gravity", C.c_int, [C.c_void_p, C.c_double]),
     ("gpb_free_velocity", C.c_int, [C.c_void_p, C.c_double, P_f64, C.c_int, P_f64]),
     ("gpb_batch_autotune", C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_int, C.POINTER(GpbControl), C.c_int,
-                                     P_i32, P_i32]),
+                                     P_i32, P_i32, P_i32]),
+    ("gpb_batch_set_mapping", C.c_int, [C.c_void_p, C.c_int]),
     ("gpb_launch_count", C.c_int64, [C.c_void_p]),
     ("gpb_last_launch_ms", C.c_double, [C.c_void_p]),
     ("gpb_config_sizes", C.c_int, [C.c_int, C.c_int64, C.c_uint32, P_i64, P_i64, P_i64, P_i64, P_i64]),

@@ -171,6 +171,10 @@ class Batch:
         """Block-cooperative packs from `min_dof` DOF up (-1 default, 0 off)."""
         _abi.check(_abi.lib().gpb_batch_set_coop(self.h, min_dof), "gpb_batch_set_coop")
 
+    def set_mapping(self, lanes_per_instance: int) -> None:
+        """Lanes per instance of GPB_FP64 steps: 1 (default) or 2..32 (body-parallel chains)."""
+        _abi.check(_abi.lib().gpb_batch_set_mapping(self.h, lanes_per_instance), "gpb_batch_set_mapping")
+
     def set_launch(self, warps_per_sm: int) -> None:
         """Resident warps per SM of the step kernel (0 = occupancy limit)."""
         _abi.check(_abi.lib().gpb_batch_set_launch(self.h, warps_per_sm), "gpb_batch_set_launch")
@@ -219,18 +223,19 @@ class Batch:
     def autotune(self, dt: float, integrator: int = _abi.SEMI_IMPLICIT_EULER,
                  precision: int = _abi.FP64, control: str = "host", tau=None, seed: int = 0,
                  resample_every: int = 10, sigma: float = 1.0, kp: float = 0.0, kd: float = 0.0,
-                 trial_steps: int = 20) -> tuple[int, int]:
+                 trial_steps: int = 20) -> tuple[int, int, int]:
         """Times the launch shapes on this batch's own step and keeps the fastest.
 
-        Returns (warps_per_sm, coop_min_dof); the state is left unchanged."""
+        Returns (warps_per_sm, coop_min_dof, lanes_per_instance); the state is
+        left unchanged."""
         mode = {"host": _abi.CONTROL_HOST_TAU, "open_loop": _abi.CONTROL_OPEN_LOOP,
                 "pd": _abi.CONTROL_PD}[control]
         t = None if tau is None else np.ascontiguousarray(tau, dtype=np.float64).ravel()
         ctl = _abi.GpbControl(mode, seed, resample_every, sigma, kp, kd, _p(t))
-        w, c = C.c_int32(), C.c_int32()
+        w, c, lanes = C.c_int32(), C.c_int32(), C.c_int32()
         _abi.check(_abi.lib().gpb_batch_autotune(self.h, dt, integrator, precision, C.byref(ctl), trial_steps,
-                                                 C.byref(w), C.byref(c)), "gpb_batch_autotune")
-        return w.value, c.value
+                                                 C.byref(w), C.byref(c), C.byref(lanes)), "gpb_batch_autotune")
+        return w.value, c.value, lanes.value
 
 
 def simulate_steps(final_time: float, dt: float) -> int:

@@ -341,8 +341,28 @@ int gpb_batch_steps_done(gpb_batch* batch, int64_t* steps);
 int gpb_synchronize(gpb_ctx* ctx);
 
 /* ---- kernel mapping ---------------------------------------------------- */
-/* One lane steps one instance (a warp steps a pack of 32), or, for the CRBA
- * route, the four warps of a block share one pack (gpb_batch_set_coop). */
+/* One lane steps one instance (a warp steps a pack of 32, the default); for
+ * the CRBA route the four warps of a block may share one pack
+ * (gpb_batch_set_coop); and a batch of serial chains may give each instance
+ * several lanes (gpb_batch_set_mapping).  gpb_batch_autotune picks among them. */
+
+/* Lanes per instance of later GPB_FP64 gpb_simulate / gpb_step calls on the
+ * CRBA route (velocity stepping excepted): 1 = one lane per instance (the
+ * default);
+ * 2, 4, 8, 16 or 32 = the body-parallel mapping, where that many lanes of a
+ * warp step one instance (32 = one warp per instance, 2 = sixteen instances
+ * per warp), each lane owning one or two consecutive bodies: the outward and
+ * inward sweeps are prefix and suffix scans across the lanes by warp
+ * shuffles, and the mass matrix and its Cholesky factor sit in shared memory
+ * with their entries dealt to the lanes.  It shortens one instance's step by
+ * up to the lane count and pays off when the batch has too few instances to
+ * fill the GPU one lane each.  Only for a batch whose every instance is a
+ * serial chain (joint k's parent is body k) of revolute, prismatic or fixed
+ * joints without cuboid colliders, with at most 2 × lanes bodies; else
+ * GPB_E_INVAL.  Results agree with the one-lane mapping to rounding (the sums
+ * run in another order); other precisions and GPB_ALGO_ABA keep one lane per
+ * instance. */
+int gpb_batch_set_mapping(gpb_batch* batch, int lanes_per_instance);
 
 /* Resident warps per SM of the persistent step kernel (one warp per pack of
  * 32 instances): 0 = as many as the kernel's registers allow (the default),
@@ -377,15 +397,19 @@ int gpb_free_velocity(gpb_batch* batch, double dt, const double* tau, int precis
 
 /* Autotuner: times `trial_steps` steps of this batch (its own mechanisms,
  * state, step size, integrator, precision and control law) for each launch
- * shape (4, 8, 12 or 16 resident warps per SM, as many as the step kernel's
- * registers allow; block-cooperative packs off or from 32 / 40 DOF when the
- * batch has such packs), keeps the fastest with
- * gpb_batch_set_launch / gpb_batch_set_coop and reports it.  The batch's q, v,
- * torques and status words are restored afterwards; results of later calls do
- * not depend on the choice (every shape computes the same bits). */
+ * shape (one lane per instance at 4, 8, 12 or 16 resident warps per SM, as
+ * many as the step kernel's registers allow; block-cooperative packs off or
+ * from 32 / 40 DOF when the batch has such packs; for GPB_FP64 CRBA on a
+ * chain batch, the body-parallel mapping at the lane counts that give each
+ * lane one or two bodies), keeps the fastest with gpb_batch_set_launch /
+ * gpb_batch_set_coop / gpb_batch_set_mapping and reports it (warps_per_sm 0
+ * for a body-parallel pick).  The batch's q, v, torques and status words are
+ * restored afterwards.  The one-lane shapes compute the same bits; the
+ * body-parallel mapping agrees with them to rounding.  Any output pointer may
+ * be NULL. */
 int gpb_batch_autotune(gpb_batch* batch, double dt, int integrator, int precision,
                        const gpb_control_params* control, int trial_steps, int* warps_per_sm,
-                       int* coop_min_dof);
+                       int* coop_min_dof, int* lanes_per_instance);
 
 /* Number of this library's kernel launches issued by the context so far. */
 int64_t gpb_launch_count(const gpb_ctx* ctx);

@@ -68,8 +68,8 @@ def test_autotune_keeps_state_and_results(ctx):
     ref = run(ctx, M, q0, v0, 0, gpb.FP64, gpb.SEMI_IMPLICIT_EULER, steps=30)
     B = Batch(M, ctx)
     B.update(q0, v0)
-    w, c = B.autotune(2e-4, gpb.SEMI_IMPLICIT_EULER, gpb.FP64, control="open_loop", seed=3, trial_steps=5)
-    assert w in (4, 8) and c in (0, 32, 40)
+    w, c, lanes = B.autotune(2e-4, gpb.SEMI_IMPLICIT_EULER, gpb.FP64, control="open_loop", seed=3, trial_steps=5)
+    assert w in (4, 8) and c in (0, 32, 40) and lanes == 1  # not a chain batch: one lane per instance
     q1, v1 = B.state()
     assert np.array_equal(q1, q0) and np.array_equal(v1, v0) and not B.status().any()
     B.simulate_steps(30, 2e-4, gpb.SEMI_IMPLICIT_EULER, gpb.FP64, control="open_loop", seed=3, sigma=1.0)
