@@ -193,10 +193,11 @@ __device__ void coop_pack(const DeviceBatch& b, const StepParams& p, int pk, Coo
   Col<double> tau{&c.d(c.L.tau)};
   int64_t done = 0;
   bool alive = in_pack && *status == 0;
+  const SlotParams sp = slot_params(b, p, 0);  // batches only (no serving jobs)
   for (int64_t s = 0; s < p.K; ++s) {
     const int64_t sidx = p.step0 + s;
     bool ht = false;
-    if (alive) ht = control(c, b, p, inst, sidx, s == 0, q, v, tin, tau);
+    if (alive) ht = control(c, b, sp, inst, sidx, s == 0, q, v, tin, tau);
     Col<double> tsrc = p.control == 0 ? tin : tau;
     const int st = coop_lane_step(ev, q, v, tsrc, ht, p.dt, p.integrator, alive);
     if (!alive) continue;

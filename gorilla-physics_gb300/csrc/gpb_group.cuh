@@ -447,24 +447,9 @@ __device__ void run_instance(const gpb::DeviceBatch& b, const gpb::StepParams& p
   using namespace gpb;
   const PackDesc pd = b.packs[pk];
   const int64_t slot = (int64_t)pk * LANES + l;
-  StepParams lp = p;
-  int64_t K = p.K;
-  if (b.jobs) {  // per-slot job of a serving pool
-    const LaneJob& j = b.jobs[slot];
-    const int64_t kc = j.chunk > 0 ? j.chunk : p.K;
-    K = j.steps_left < kc ? j.steps_left : kc;
-    if (K <= 0) return;
-    lp.step0 = j.step_index;
-    lp.dt = j.dt;
-    lp.integrator = j.integrator;
-    lp.control = j.control;
-    lp.seed = j.seed;
-    lp.resample = j.resample;
-    lp.sigma = j.sigma;
-    lp.kp = j.kp;
-    lp.kd = j.kd;
-    lp.tau_mode = j.tau_mode;
-  }
+  const SlotParams lp = slot_params(b, p, slot);  // the launch's, or a serving job's
+  const int64_t K = lp.K;
+  if (K <= 0) return;
   const int32_t* li = b.laneI + pd.lane * LANES + l;
   Inst<S> g;
   g.G = G;

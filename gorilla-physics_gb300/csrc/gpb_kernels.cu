@@ -1087,10 +1087,53 @@ __device__ __forceinline__ LaneCtx<R> make_ctx(const DeviceBatch& b, const PackD
   return c;
 }
 
+// Step settings and control law of one slot: the launch's, or the request's
+// own when the slot holds a serving job.  Built field by field: a modified
+// copy of the whole StepParams (136 bytes) was seen to read the launch's dt
+// instead of the assigned one in the step kernel (nvcc 13.0, sm_103a), and
+// plain per-field values do not depend on how such a copy is lowered.
+struct SlotParams {
+  int64_t K, step0;
+  double dt, sigma, kp, kd;
+  uint32_t seed;
+  int32_t integrator, control, resample, tau_mode;
+};
+__device__ __forceinline__ SlotParams slot_params(const DeviceBatch& b, const StepParams& p, int64_t slot) {
+  SlotParams s;
+  if (b.jobs) {
+    const LaneJob& j = b.jobs[slot];
+    const int64_t kc = j.chunk > 0 ? j.chunk : p.K;
+    s.K = j.steps_left < kc ? j.steps_left : kc;
+    s.step0 = j.step_index;
+    s.dt = j.dt;
+    s.sigma = j.sigma;
+    s.kp = j.kp;
+    s.kd = j.kd;
+    s.seed = j.seed;
+    s.integrator = j.integrator;
+    s.control = j.control;
+    s.resample = j.resample;
+    s.tau_mode = j.tau_mode;
+  } else {
+    s.K = p.K;
+    s.step0 = p.step0;
+    s.dt = p.dt;
+    s.sigma = p.sigma;
+    s.kp = p.kp;
+    s.kd = p.kd;
+    s.seed = p.seed;
+    s.integrator = p.integrator;
+    s.control = p.control;
+    s.resample = p.resample;
+    s.tau_mode = p.tau_mode;
+  }
+  return s;
+}
+
 // Control law before a step.
 template <typename R>
 __device__ __forceinline__ bool control(const LaneCtx<R>& c, const DeviceBatch& b,
-                                        const StepParams& p, int64_t inst, int64_t sidx, bool first,
+                                        const SlotParams& p, int64_t inst, int64_t sidx, bool first,
                                         Col<double> q, Col<double> v, Col<double> tin,
                                         Col<double> tau) {
   if (p.control == 1) {  // open loop
@@ -1177,24 +1220,9 @@ __global__ void __launch_bounds__(128, PREC == 1 ? GPB_MIXED_MIN_BLOCKS : 1) sim
     const int64_t slot = (int64_t)pk * LANES + lane;
     // per-slot job of a serving pool: the request's own K, step counter, step
     // size, integrator and control law
-    StepParams lp = p;
-    int64_t K = p.K;
-    if (b.jobs) {
-      const LaneJob& j = b.jobs[slot];
-      const int64_t kc = j.chunk > 0 ? j.chunk : p.K;
-      K = j.steps_left < kc ? j.steps_left : kc;
-      if (K <= 0) continue;
-      lp.step0 = j.step_index;
-      lp.dt = j.dt;
-      lp.integrator = j.integrator;
-      lp.control = j.control;
-      lp.seed = j.seed;
-      lp.resample = j.resample;
-      lp.sigma = j.sigma;
-      lp.kp = j.kp;
-      lp.kd = j.kd;
-      lp.tau_mode = j.tau_mode;
-    }
+    const SlotParams lp = slot_params(b, p, slot);
+    const int64_t K = lp.K;
+    if (K <= 0) continue;
     const auto ev = EvalOf<PREC>::make(b, pd, lane);
     const auto& c = ev.c;
     int32_t* status = b.status + slot;

@@ -152,6 +152,36 @@ def test_server_matches_batch_api(ctx):
 
 
 @pytest.mark.gpu
+def test_requests_keep_their_own_settings(ctx):
+    """Requests in one pool with different step sizes, integrators and control
+    laws each run with their own (the job's, not the launch's): every one
+    equals the same instance as a batch of one with its settings."""
+    M, q0, v0, _ = Model.from_config(0, 6, seed=7)
+    qo, vo, _ = M.offsets()
+    cases = [(1e-3, gpb.SEMI_IMPLICIT_EULER, "host"), (4e-4, gpb.RUNGE_KUTTA_4, "open_loop"),
+             (2e-3, gpb.RUNGE_KUTTA_2, "pd"), (5e-4, gpb.SEMI_IMPLICIT_EULER, "open_loop"),
+             (1e-3, gpb.RUNGE_KUTTA_4, "host"), (7e-4, gpb.RUNGE_KUTTA_2, "open_loop")]
+    tau = np.full(vo[-1], 0.3)
+    S = Server(ctx, [SlotClass(2, 2, 2, packs=1)], precision=gpb.FP64, chunk_steps=29)
+    ids = [int(S.submit(M, i, 1, q0, v0, dt=dt, steps=90 + 7 * i, integrator=integ, control=ctl,
+                        tau=tau if ctl == "pd" else None, seed=5 + i, kp=40.0, kd=1.5, keys=0)[0])
+           for i, (dt, integ, ctl) in enumerate(cases)]
+    S.drain(100000)
+    out = [S.result(r) for r in ids]
+    S.close()
+    for i, (dt, integ, ctl) in enumerate(cases):
+        B = Batch(M.subset([i]), ctx)
+        B.update(q0[qo[i]:qo[i + 1]], v0[vo[i]:vo[i + 1]])
+        B.simulate_steps(90 + 7 * i, dt, integ, gpb.FP64, control=ctl,
+                         tau=tau[vo[i]:vo[i + 1]] if ctl == "pd" else None, seed=5 + i, kp=40.0, kd=1.5)
+        qb, vb = B.state()
+        B.close()
+        qs, vs, st, done, _ = out[i]
+        assert st == 0 and done == 90 + 7 * i, i
+        assert np.array_equal(qb, qs) and np.array_equal(vb, vs), i
+
+
+@pytest.mark.gpu
 def test_admission_respects_capacity_fifo(ctx):
     """One pack of 32 slots, 80 equal requests: they run in submission order, 32 at a time."""
     M, q0, v0, _ = Model.from_config(0, 80, seed=2)
