@@ -288,15 +288,26 @@ def run_reference_cuboids(args):
 VMAX_BOUNDED = 1e4
 
 
-def qdd_error(B, gpb, precision, algorithm, where):
+def qdd_error(B, gpb, precision, algorithm, where, lanes=1):
     """Per-instance q̈ error of (precision, algorithm) against the FP64 form of
     the reference's route (CRBA + solve), at the batch's current state.  That
-    FP64 form agrees with the oracle to ≤ max(1e-10, 5e-15 cond(M))."""
+    FP64 form agrees with the oracle to ≤ max(1e-10, 5e-15 cond(M)).  With
+    several lanes per instance the form's q̈ is read from one step of the
+    body-parallel mapping itself: semi-implicit Euler evaluates q̈ at the
+    current state, and (v1 − v0) / dt recovers it to |v|·ε/dt."""
     ok = B.status() == 0
     B.set_algorithm(gpb.ALGO_CRBA)
     a = B.dynamics_continuous(None, precision=gpb.FP64)
     B.set_algorithm(algorithm)
-    b = B.dynamics_continuous(None, precision=precision)
+    if lanes > 1:
+        B.set_mapping(lanes)
+        qs, vs = B.state()
+        dt = 1e-3
+        B.step(dt, None, gpb.SEMI_IMPLICIT_EULER, precision)
+        b = (B.state()[1] - vs) / dt
+        B.update(qs, vs)
+    else:
+        b = B.dynamics_continuous(None, precision=precision)
     vo = B.v_offset
     _, vel = B.state()
     err, rel, vmax = [], [], []
@@ -393,6 +404,8 @@ def run_gpu(args):
         else:
             w, c, lanes = B.autotune(dt, 0, prec, trial_steps=10, **kw)
         launch[name] = {"warps_per_sm": w, "coop_min_dof": c, "lanes_per_instance": lanes}
+        if lanes > 1:  # the body-parallel mapping factors H whatever the algorithm setting
+            inst_flops = MODES["fp64_crba"][2]
         if args.warmup:
             B.simulate_steps(args.warmup, dt, 0, prec, step0=0, **kw)
         barrier()
@@ -411,10 +424,11 @@ def run_gpu(args):
         bad = int(np.sum(B.status() != 0))
         done = B.steps_done()
         if name != "fp64_crba":  # q̈ error at the final state of this form's own trajectory
-            errs[name] = {"final": qdd_error(B, gpb, prec, algo, f"after this form's {args.steps}-step timed run")}
+            errs[name] = {"final": qdd_error(B, gpb, prec, algo, f"after this form's {args.steps}-step timed run",
+                                             lanes)}
         # only completed instance-steps count (a diverged instance freezes)
         results[name] = {"kernel_ms": kernel_ms, "wall_s": wall, "clocks": clk.summary(),
-                         "failed_instances": bad, "launches": timed_launches,
+                         "failed_instances": bad, "launches": timed_launches, "lanes": lanes,
                          "done": reduce_sum(float(done.sum())),
                          "flops": reduce_sum(float(np.dot(done, inst_flops.astype(np.float64))))}
         if lanes > 1 and world == 1:
@@ -442,7 +456,8 @@ def run_gpu(args):
     B.clear_status()
     for name in errs:
         prec, algo, _ = MODES[name]
-        errs[name]["initial"] = qdd_error(B, gpb, prec, algo, "the configuration's initial states")
+        errs[name]["initial"] = qdd_error(B, gpb, prec, algo, "the configuration's initial states",
+                                          launch[name]["lanes_per_instance"])
     # headline: the fastest form that meets the stated bound (every instance
     # whose trajectory is not blown up within 1e-5 at both states); the FP64
     # forms are exact to round-off
@@ -517,7 +532,8 @@ def run_gpu(args):
     def roof(name, res):
         ach = res["flops"] / (res["kernel_ms"] * 1e-3) / 1e12
         per = res["flops"] / max(res["done"], 1.0)
-        t = traffic_per.get(name)
+        # the ncu table describes the one-lane kernels
+        t = traffic_per.get(name) if res["lanes"] == 1 else None
         if name == "mixed" and t and "warp_instructions_per_instance_step" in t and not args.mix_chains:
             wi = t["warp_instructions_per_instance_step"]
             ach_i = wi * res["done"] / (res["kernel_ms"] * 1e-3) / 1e9
@@ -529,7 +545,8 @@ def run_gpu(args):
         else:
             out = {"bound": "fp64", "achieved": ach, "peak": p64, "unit": "TFLOP/s", "frac": ach / p64,
                    "traffic": None, "peak_source": "measured FP64 FMA microbenchmark (gpb_fma_peak), this run",
-                   "work": f"{per:.0f} FP64 flops per completed instance-step (mean): {WORK[name]}"}
+                   "work": f"{per:.0f} FP64 flops per completed instance-step (mean): "
+                           + (WORK[name] if res["lanes"] == 1 else WORK["fp64_crba"])}
         if t and not args.mix_chains:
             bytes_launch = t["dram_bytes_per_instance_step"] * res["done"]
             out["traffic"] = bytes_launch
@@ -541,10 +558,20 @@ def run_gpu(args):
         return out
 
     DTYPE = {"fp64_crba": "f64", "fp64": "f64",
-             "mixed": "f32 kinematics/bias + double-f32 articulated inertias + f64 state",
+             "mixed": "f32 kinematics/bias + double-f32 articulated inertias + f64 state"
+             if launch.get("mixed", {}).get("lanes_per_instance", 1) == 1
+             else "f64 (the body-parallel mapping computes in FP64 for GPB_MIXED requests)",
              "refined": "f32 solve + f64 residual refinement + f64 state"}
-    ALGO = {"fp64_crba": "CRBA + Cholesky (the reference's route)", "fp64": "articulated-body algorithm",
-            "mixed": "articulated-body algorithm", "refined": "CRBA + Cholesky, iterative refinement"}
+    ALGO0 = {"fp64_crba": "CRBA + Cholesky (the reference's route)", "fp64": "articulated-body algorithm",
+             "mixed": "articulated-body algorithm", "refined": "CRBA + Cholesky, iterative refinement"}
+
+    def algo_label(name):
+        lanes = (launch.get(name) or {}).get("lanes_per_instance", 1)
+        if lanes == 1:
+            return ALGO0[name]
+        return f"CRBA + Cholesky in FP64, body-parallel: {lanes} lanes per instance"
+
+    ALGO = {k: algo_label(k) for k in ALGO0}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["kernel_ms"] / args.steps,

@@ -24,10 +24,15 @@
 //   solve     Cholesky H = L Lᵀ, right-looking, each column's trailing update
 //             dealt evenly to the lanes, then the two triangular solves
 //             (src/dynamics.rs:255-276 solves the same system by LU).
-// The arithmetic is FP64 throughout: this is the plain form, for instances too
-// few to fill the GPU one lane each, where the latency of one instance's step
-// sets the rate.  Its sums run in another order than the one-lane sweeps, so
-// the two mappings agree to rounding, not bit for bit.
+// It serves instances too few to fill the GPU one lane each, where the
+// latency of one instance's step sets the rate.  The arithmetic is FP64 for
+// GPB_FP64 and GPB_MIXED requests alike: a double-float version of this
+// kernel (every sum and product on the FP32 pipes) measured no faster on
+// GB300 — 1,024 chains 4.6 against 4.7 M instance-steps/s, a lone 48-body
+// chain 166 against 188 µs a step — since one instance's chain of dependent
+// operations and barriers, not the FP64 pipe's throughput, sets its step
+// time.  Its sums run in another order than the one-lane sweeps, so the two
+// mappings agree to rounding, not bit for bit.
 //
 // Every shuffle and __syncwarp of a group runs under the group's own mask and
 // in control flow that depends only on the instance (never on the lane), so
@@ -391,11 +396,11 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
     }
     const double r = rsqrt(d);
     for (int i = k + 1 + t; i < n; i += G) H[off(i) + k] *= r;
-    if (t == 0) {
+    __syncwarp(gm);
+    if (t == 0) {  // every lane has read the pivot: the barrier above orders this write after them
       H[off(k) + k] = d * r;
       dinv[k] = r;
     }
-    __syncwarp(gm);
     // trailing block rows k+1 … n−1, entry (a, c), c ≤ a, to lane (a(a+1)/2 + c) mod G
     const int m = n - k - 1;
     int a = 0, c = t;

@@ -607,8 +607,10 @@ static int run_simulate(gpb_batch* b, double dt, int64_t K, int64_t step0, int i
     p.history = b->hist.p;
     p.record_every = record_every;
   }
-  // body-parallel mapping: GPB_FP64 steps of a chain batch, when chosen
-  const int gs = precision == GPB_FP64 && b->algorithm == GPB_ALGO_CRBA && integrator != GPB_VELOCITY_STEPPING &&
+  // body-parallel mapping (GPB_FP64 or GPB_MIXED steps of a chain batch), when
+  // chosen; it factors H in FP64 whatever the algorithm setting, which
+  // selects the one-lane route
+  const int gs = (precision == GPB_FP64 || precision == GPB_MIXED) && integrator != GPB_VELOCITY_STEPPING &&
                          b->lanes > 1
                      ? group_bodies_per_lane(b, b->lanes)
                      : 0;
@@ -687,8 +689,8 @@ extern "C" int gpb_batch_autotune(gpb_batch* b, double dt, int integrator, int p
         b->packs_h[0].minnv >= 32)
       for (int c : {40, 32}) cand.push_back({w, c, 1});
   }
-  // body-parallel chains (the CRBA route): the group sizes with one or two bodies per lane
-  if (precision == GPB_FP64 && b->algorithm == GPB_ALGO_CRBA && integrator != GPB_VELOCITY_STEPPING)
+  // body-parallel chains: the group sizes with one or two bodies per lane
+  if ((precision == GPB_FP64 || precision == GPB_MIXED) && integrator != GPB_VELOCITY_STEPPING)
     for (int l = 2; l <= LANES; l *= 2)
       if (group_bodies_per_lane(b, l) && (l < 2 * b->nb_max || l == 2)) cand.push_back({0, 0, l});
   double best = 1e300;

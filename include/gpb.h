@@ -346,8 +346,8 @@ int gpb_synchronize(gpb_ctx* ctx);
  * (gpb_batch_set_coop); and a batch of serial chains may give each instance
  * several lanes (gpb_batch_set_mapping).  gpb_batch_autotune picks among them. */
 
-/* Lanes per instance of later GPB_FP64 gpb_simulate / gpb_step calls on the
- * CRBA route (velocity stepping excepted): 1 = one lane per instance (the
+/* Lanes per instance of later GPB_FP64 and GPB_MIXED gpb_simulate / gpb_step
+ * calls (velocity stepping excepted): 1 = one lane per instance (the
  * default);
  * 2, 4, 8, 16 or 32 = the body-parallel mapping, where that many lanes of a
  * warp step one instance (32 = one warp per instance, 2 = sixteen instances
@@ -359,9 +359,11 @@ int gpb_synchronize(gpb_ctx* ctx);
  * fill the GPU one lane each.  Only for a batch whose every instance is a
  * serial chain (joint k's parent is body k) of revolute, prismatic or fixed
  * joints without cuboid colliders, with at most 2 × lanes bodies; else
- * GPB_E_INVAL.  Results agree with the one-lane mapping to rounding (the sums
- * run in another order); other precisions and GPB_ALGO_ABA keep one lane per
- * instance. */
+ * GPB_E_INVAL.  The mapping builds and factors the mass matrix (the CRBA route)
+ * in FP64 whatever gpb_batch_set_algorithm chose (which then selects the
+ * one-lane route only) and for GPB_MIXED requests too; its results agree
+ * with the one-lane FP64 forms to rounding (the sums run in another order).
+ * GPB_MIXED_REFINED keeps one lane per instance. */
 int gpb_batch_set_mapping(gpb_batch* batch, int lanes_per_instance);
 
 /* Resident warps per SM of the persistent step kernel (one warp per pack of
@@ -399,9 +401,9 @@ int gpb_free_velocity(gpb_batch* batch, double dt, const double* tau, int precis
  * state, step size, integrator, precision and control law) for each launch
  * shape (one lane per instance at 4, 8, 12 or 16 resident warps per SM, as
  * many as the step kernel's registers allow; block-cooperative packs off or
- * from 32 / 40 DOF when the batch has such packs; for GPB_FP64 CRBA on a
- * chain batch, the body-parallel mapping at the lane counts that give each
- * lane one or two bodies), keeps the fastest with gpb_batch_set_launch /
+ * from 32 / 40 DOF when the batch has such packs; for GPB_FP64 and GPB_MIXED
+ * on a chain batch, the body-parallel mapping at the lane counts that give
+ * each lane one or two bodies), keeps the fastest with gpb_batch_set_launch /
  * gpb_batch_set_coop / gpb_batch_set_mapping and reports it (warps_per_sm 0
  * for a body-parallel pick).  The batch's q, v, torques and status words are
  * restored afterwards.  The one-lane shapes compute the same bits; the

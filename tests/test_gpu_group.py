@@ -1,6 +1,6 @@
 """Body-parallel mapping of serial chains (gpb_batch_set_mapping): 2–32 lanes of
 a warp step one instance, the sweeps as warp-shuffle scans, the mass matrix and
-its Cholesky factor in shared memory.  FP64 throughout.
+its Cholesky factor in shared memory; FP64 (also for GPB_MIXED requests).
 
 Bounds, against the oracle (the reference's algorithm with a Cholesky solve):
   * one step: q, v within 1e-10 · max(|x|, 1), as the one-lane mapping;
@@ -227,9 +227,10 @@ def test_failures_are_flagged_and_frozen(ctx):
 
 def test_mapping_rules(ctx):
     """Lane counts: 1 or a power of two in [2, 32] with at most two bodies per
-    lane; only chain batches; other precisions and the articulated-body route
-    keep one lane per instance (bit-identical to a batch that never set the
-    mapping)."""
+    lane; only chain batches.  GPB_MIXED_REFINED keeps one lane per instance
+    (bit-identical to a batch that never set the mapping); under the
+    articulated-body setting the mapping still factors H, in agreement with the
+    one-lane articulated-body route to rounding."""
     M, q0, v0, _ = Model.from_config(1, 40, seed=6)  # up to 48 bodies: only 32 lanes give ≤ 2 per lane
     nb_max = int(np.max(np.diff(M.joint_offset)))
     B = Batch(M, ctx)
@@ -241,20 +242,18 @@ def test_mapping_rules(ctx):
             B.set_mapping(16)
     B.set_mapping(32)
     B.update(q0, v0)
-    B.simulate_steps(20, 5e-4, gpb.SEMI_IMPLICIT_EULER, gpb.MIXED)
+    B.simulate_steps(20, 5e-4, gpb.SEMI_IMPLICIT_EULER, gpb.MIXED_REFINED)
     R = Batch(M, ctx)
-    R.set_algorithm(gpb.ALGO_CRBA)
     R.update(q0, v0)
-    R.simulate_steps(20, 5e-4, gpb.SEMI_IMPLICIT_EULER, gpb.MIXED)
+    R.simulate_steps(20, 5e-4, gpb.SEMI_IMPLICIT_EULER, gpb.MIXED_REFINED)
     np.testing.assert_array_equal(B.q, R.q)
-    # the articulated-body route keeps one lane per instance too
     B.set_algorithm(gpb.ALGO_ABA)
     R.set_algorithm(gpb.ALGO_ABA)
     B.update(q0, v0)
     R.update(q0, v0)
     B.simulate_steps(20, 5e-4)
     R.simulate_steps(20, 5e-4)
-    np.testing.assert_array_equal(B.q, R.q)
+    assert rel_err(B.q, R.q) < 1e-10 and rel_err(B.v, R.v) < 1e-10
     B.close()
     R.close()
     Q, _, _, _ = Model.from_config(3, 4, seed=1)  # quadrupeds: trees with a floating base
@@ -263,6 +262,23 @@ def test_mapping_rules(ctx):
         C.set_mapping(16)
     C.set_mapping(1)
     C.close()
+
+
+def test_mixed_requests_run_fp64(ctx):
+    """A GPB_MIXED step on the body-parallel mapping is its FP64 computation
+    (bit-identical to a GPB_FP64 step on it), under either algorithm setting."""
+    M, q0, v0, _ = Model.from_config(1, 96, seed=13)
+    for algo in (gpb.ALGO_CRBA, gpb.ALGO_ABA):
+        out = []
+        for prec in (gpb.FP64, gpb.MIXED):
+            B = Batch(M, ctx)
+            B.set_algorithm(algo)
+            B.set_mapping(32)
+            B.update(q0, v0)
+            B.simulate_steps(50, 5e-4, gpb.SEMI_IMPLICIT_EULER, prec, "open_loop", seed=2)
+            out.append(B.state())
+            B.close()
+        assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1]), algo
 
 
 def test_autotune_chooses_among_mappings(ctx):
