@@ -104,11 +104,110 @@ __device__ __forceinline__ SI<double> si_zero() {
   return z;
 }
 
+// The values the three scans carry, their shuffles and combinations.
+struct VA {  // (body velocity, bias acceleration) sums along the chain
+  SV<double> V, A;
+};
+struct IFc {  // (composite inertia, joint force) sums from the tip
+  SI<double> I;
+  SV<double> F;
+};
+__device__ __forceinline__ Xf up1(unsigned m, const Xf& x, int d, int W) { return up_xf(m, x, d, W); }
+__device__ __forceinline__ VA up1(unsigned m, const VA& x, int d, int W) {
+  return {up_sv(m, x.V, d, W), up_sv(m, x.A, d, W)};
+}
+__device__ __forceinline__ IFc dn1(unsigned m, const IFc& x, int d, int W) {
+  return {dn_si(m, x.I, d, W), dn_sv(m, x.F, d, W)};
+}
+// left-to-right combination: first a's segment of the chain, then b's
+__device__ __forceinline__ Xf comb(const Xf& a, const Xf& b) { return compose(a, b); }
+__device__ __forceinline__ VA comb(const VA& a, const VA& b) {
+  return {a.V + b.V, a.A + b.A + gpb::crm(a.V, b.V)};
+}
+__device__ __forceinline__ IFc add(const IFc& a, const IFc& b) {
+  IFc r = a;
+  gpb::iadd(r.I, b.I);
+  r.F = a.F + b.F;
+  return r;
+}
+
+// Barrier and OR-reduction of a group: its lanes of one warp, or (BLK) the
+// whole block, which then steps one instance.
+template <bool BLK>
+__device__ __forceinline__ void gsync(unsigned gm) {
+  if constexpr (BLK)
+    __syncthreads();
+  else
+    __syncwarp(gm);
+}
+template <bool BLK>
+__device__ __forceinline__ unsigned gor(unsigned gm, unsigned v) {
+  if constexpr (BLK) {  // __syncthreads_or answers any-nonzero, not the OR of the bits: one per status bit
+    unsigned r = 0;
+#pragma unroll
+    for (int bit = 0; bit < 4; ++bit)
+      if (__syncthreads_or((int)(v & (1u << bit)))) r |= 1u << bit;
+    return r;
+  } else {
+    return __reduce_or_sync(gm, v);
+  }
+}
+
+// Exclusive prefix scan of x over the group's lanes (the combination of the
+// values of lanes 0 … t−1; ident for lane 0): Kogge–Stone by shuffles within
+// a warp; with BLK the warps' totals then meet in shared memory (wsm, one
+// slot per warp), each warp combining those of the warps before it.
+template <bool BLK, typename T>
+__device__ __forceinline__ T excl_prefix(T x, int t, int G, unsigned gm, const T& ident, T* wsm) {
+  const int W = BLK ? 32 : G, lane = BLK ? (t & 31) : t;
+  for (int d = 1; d < W; d <<= 1) {
+    const T y = up1(gm, x, d, W);
+    if (lane >= d) x = comb(y, x);
+  }
+  T pre = ident;
+  if constexpr (BLK) {
+    const int w = t >> 5;
+    if (lane == W - 1) wsm[w] = x;
+    __syncthreads();
+    for (int u = 0; u < w; ++u) pre = comb(pre, wsm[u]);
+    __syncthreads();  // the slots are reused by the next scan
+    x = comb(pre, x);
+  }
+  T e = up1(gm, x, 1, W);
+  if (lane == 0) e = pre;
+  return e;
+}
+// Exclusive suffix sum over the group's lanes (lanes t+1 … G−1; zero for the
+// last), the same way from the other end.
+template <bool BLK>
+__device__ __forceinline__ IFc excl_suffix(IFc x, int t, int G, unsigned gm, const IFc& zero, IFc* wsm) {
+  const int W = BLK ? 32 : G, lane = BLK ? (t & 31) : t;
+  for (int d = 1; d < W; d <<= 1) {
+    const IFc y = dn1(gm, x, d, W);
+    if (lane + d < W) x = add(x, y);
+  }
+  IFc post = zero;
+  if constexpr (BLK) {
+    const int w = t >> 5, nw = G >> 5;
+    if (lane == 0) wsm[w] = x;
+    __syncthreads();
+    for (int u = nw - 1; u > w; --u) post = add(post, wsm[u]);
+    __syncthreads();
+    x = add(x, post);
+  }
+  IFc e = dn1(gm, x, 1, W);
+  if (lane == W - 1) e = post;
+  return e;
+}
+
 // Doubles of shared memory per instance for up to n DOF: packed lower
 // triangle of H (row i at i(i+1)/2), the world motion subspaces and the
 // columns Ic_i S_i (6 n each, component-major), the right-hand side, the
 // intermediate vector of the solves and the reciprocal pivots (n each).
 __host__ __device__ inline int smem_words(int n) { return n * (n + 1) / 2 + 15 * n; }
+// A block per instance also keeps its warps' scan totals: 4 warps × 16 doubles.
+constexpr int BLK_WARPS = 4;
+constexpr int BLK_SCAN_WORDS = BLK_WARPS * 16;
 
 __device__ __forceinline__ int off(int i) { return (i * (i + 1)) >> 1; }
 
@@ -222,7 +321,7 @@ __device__ __forceinline__ void contacts(const Inst<S>& g, int s, const Xf& X, c
 // One dynamics evaluation of the group's instance: q, v, τ of the lane's
 // bodies → q̈ of the lane's bodies.  Returns GPB status bits (the same in
 // every lane of the group).
-template <int S>
+template <int S, bool BLK>
 __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], const double (&vin)[S],
                                  const double (&tauin)[S], bool ht, bool springs, double (&qdd)[S]) {
   const Inst<S> g = gin;  // private copies: kept in registers, not read through the references
@@ -242,13 +341,9 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
     const Xf J = g.body(s) < g.nb ? joint_xf(g, s, q[s]) : identity();
     X[s] = s == 0 ? J : compose(X[s - 1], J);
   }
+  double* const wsm = g.sm + smem_words(g.nvp);  // BLK: the warps' scan totals
   {
-    Xf T = X[S - 1];
-    for (int d = 1; d < G; d <<= 1) {
-      const Xf Y = up_xf(gm, T, d, G);
-      if (t >= d) T = compose(Y, T);
-    }
-    Xf E = up_xf(gm, T, 1, G);
+    const Xf E = excl_prefix<BLK>(X[S - 1], t, G, gm, identity(), reinterpret_cast<Xf*>(wsm));
     if (t > 0) {
 #pragma unroll
       for (int s = 0; s < S; ++s) X[s] = compose(E, X[s]);
@@ -276,16 +371,9 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
   }
   // ---- (V, A) scan
   {
-    SV<double> TV = V[S - 1], TA = A[S - 1];
-    for (int d = 1; d < G; d <<= 1) {
-      const SV<double> YV = up_sv(gm, TV, d, G), YA = up_sv(gm, TA, d, G);
-      if (t >= d) {
-        TA = YA + TA + gpb::crm(YV, TV);
-        TV = YV + TV;
-      }
-    }
-    SV<double> EV = up_sv(gm, TV, 1, G), EA = up_sv(gm, TA, 1, G);
-    if (t == 0) EV = EA = sv_zero();
+    const VA E = excl_prefix<BLK>(VA{V[S - 1], A[S - 1]}, t, G, gm, VA{sv_zero(), sv_zero()},
+                                  reinterpret_cast<VA*>(wsm));
+    const SV<double> EV = E.V, EA = E.A;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       A[s] = EA + A[s] + gpb::crm(EV, V[s]);
@@ -318,23 +406,13 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
     F[s] = F[s] + F[s + 1];
   }
   {
-    SI<double> TI = Ic[0];
-    SV<double> TF = F[0];
-    for (int d = 1; d < G; d <<= 1) {
-      const SI<double> YI = dn_si(gm, TI, d, G);
-      const SV<double> YF = dn_sv(gm, TF, d, G);
-      if (t + d < G) {
-        gpb::iadd(TI, YI);
-        TF = TF + YF;
-      }
-    }
-    const SI<double> EI = dn_si(gm, TI, 1, G);
-    const SV<double> EF = dn_sv(gm, TF, 1, G);
+    const IFc E = excl_suffix<BLK>(IFc{Ic[0], F[0]}, t, G, gm, IFc{si_zero(), sv_zero()},
+                                   reinterpret_cast<IFc*>(wsm));
     if (t + 1 < G) {
 #pragma unroll
       for (int s = 0; s < S; ++s) {
-        gpb::iadd(Ic[s], EI);
-        F[s] = F[s] + EF;
+        gpb::iadd(Ic[s], E.I);
+        F[s] = F[s] + E.F;
       }
     }
   }
@@ -365,7 +443,7 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
     // (no armature: dynamics.rs's mass matrix has none; only free_velocity adds it)
     H[off(i) + i] = gpb::sdot2(Fi, Sw[s]);
   }
-  __syncwarp(gm);
+  gsync<BLK>(gm);
   // ---- strictly lower triangle of H, entry e = i(i−1)/2 + j to lane e mod G
   {
     int i = 1, j = t;
@@ -388,7 +466,7 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
   // ---- Cholesky H = L Lᵀ in place (right-looking)
   int st = 0;
   for (int k = 0; k < n; ++k) {
-    __syncwarp(gm);
+    gsync<BLK>(gm);
     double d = H[off(k) + k];
     if (!(d > 0.0)) {
       st |= 2;  // GPB_ST_CHOL_FAIL; continue with a unit pivot, as the one-lane factor does
@@ -396,7 +474,7 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
     }
     const double r = rsqrt(d);
     for (int i = k + 1 + t; i < n; i += G) H[off(i) + k] *= r;
-    __syncwarp(gm);
+    gsync<BLK>(gm);
     if (t == 0) {  // every lane has read the pivot: the barrier above orders this write after them
       H[off(k) + k] = d * r;
       dinv[k] = r;
@@ -420,18 +498,18 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
   }
   // ---- L y = rhs (y into z), then Lᵀ q̈ = y (into x)
   for (int k = 0; k < n; ++k) {
-    __syncwarp(gm);
+    gsync<BLK>(gm);
     const double y = x[k] * dinv[k];
     for (int i = k + 1 + t; i < n; i += G) x[i] = fma(-H[off(i) + k], y, x[i]);
     if (t == 0) z[k] = y;
   }
   for (int k = n - 1; k >= 0; --k) {
-    __syncwarp(gm);
+    gsync<BLK>(gm);
     const double xk = z[k] * dinv[k];
     for (int i = t; i < k; i += G) z[i] = fma(-H[off(k) + i], xk, z[i]);
     if (t == 0) x[k] = xk;
   }
-  __syncwarp(gm);
+  gsync<BLK>(gm);
 #pragma unroll
   for (int s = 0; s < S; ++s) {
     qdd[s] = 0.0;
@@ -440,13 +518,13 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
       if (!isfinite(qdd[s])) st |= 1;  // GPB_ST_NONFINITE
     }
   }
-  __syncwarp(gm);  // the next evaluation overwrites x
-  return (int)__reduce_or_sync(gm, (unsigned)st);
+  gsync<BLK>(gm);  // the next evaluation overwrites x
+  return (int)gor<BLK>(gm, (unsigned)st);
 }
 
 // All K steps of one instance (pack pk, lane l) by its group: the integrators
 // of lane_step (src/integrators.rs:25-39,177-319) on the lane's own bodies.
-template <int S>
+template <int S, bool BLK>
 __device__ void run_instance(const gpb::DeviceBatch& b, const gpb::StepParams& p, int pk, int l, int G, int t,
                              unsigned gm, double* sm) {
   using namespace gpb;
@@ -523,7 +601,7 @@ __device__ void run_instance(const gpb::DeviceBatch& b, const gpb::StepParams& p
     double k1[S];
     int st;
     if (lp.integrator == 0) {  // semi-implicit Euler
-      st = eval<S>(g, q, v, tau, ht, true, k1);
+      st = eval<S, BLK>(g, q, v, tau, ht, true, k1);
       if (!st) {
 #pragma unroll
         for (int k = 0; k < S; ++k) {
@@ -533,14 +611,14 @@ __device__ void run_instance(const gpb::DeviceBatch& b, const gpb::StepParams& p
       }
     } else if (lp.integrator == 1) {  // RK2: every stage from (q0, v0), positions with v0
       double qs[S], vs[S];
-      st = eval<S>(g, q, v, tau, ht, true, k1);
+      st = eval<S, BLK>(g, q, v, tau, ht, true, k1);
       if (!st) {
 #pragma unroll
         for (int k = 0; k < S; ++k) {
           vs[k] = v[k] + k1[k] * (dt / 2.0);
           qs[k] = q[k] + v[k] * (dt / 2.0);
         }
-        st = eval<S>(g, qs, vs, tau, ht, true, k1);
+        st = eval<S, BLK>(g, qs, vs, tau, ht, true, k1);
       }
       if (!st) {
 #pragma unroll
@@ -551,7 +629,7 @@ __device__ void run_instance(const gpb::DeviceBatch& b, const gpb::StepParams& p
       }
     } else {  // RK4 as the reference writes it
       double qs[S], vs[S], f[S];
-      st = eval<S>(g, q, v, tau, ht, true, k1);
+      st = eval<S, BLK>(g, q, v, tau, ht, true, k1);
       if (!st) {
 #pragma unroll
         for (int k = 0; k < S; ++k) {
@@ -559,7 +637,7 @@ __device__ void run_instance(const gpb::DeviceBatch& b, const gpb::StepParams& p
           vs[k] = v[k] + k1[k] * (dt / 2.0);
           qs[k] = q[k] + v[k] * (dt / 2.0);
         }
-        st = eval<S>(g, qs, vs, tau, ht, true, k1);
+        st = eval<S, BLK>(g, qs, vs, tau, ht, true, k1);
       }
       if (!st) {
 #pragma unroll
@@ -567,7 +645,7 @@ __device__ void run_instance(const gpb::DeviceBatch& b, const gpb::StepParams& p
           f[k] = f[k] + k1[k] * 2.0;
           vs[k] = v[k] + k1[k] * (dt / 2.0);
         }
-        st = eval<S>(g, qs, vs, tau, ht, true, k1);
+        st = eval<S, BLK>(g, qs, vs, tau, ht, true, k1);
       }
       if (!st) {
 #pragma unroll
@@ -576,7 +654,7 @@ __device__ void run_instance(const gpb::DeviceBatch& b, const gpb::StepParams& p
           vs[k] = v[k] + k1[k] * dt;
           qs[k] = q[k] + v[k] * dt;
         }
-        st = eval<S>(g, qs, vs, tau, ht, true, k1);
+        st = eval<S, BLK>(g, qs, vs, tau, ht, true, k1);
       }
       if (!st) {
 #pragma unroll
@@ -595,7 +673,7 @@ __device__ void run_instance(const gpb::DeviceBatch& b, const gpb::StepParams& p
 #pragma unroll
     for (int k = 0; k < S; ++k)
       if (!isfinite(q[k])) bad = 1;
-    status |= (int32_t)__reduce_or_sync(gm, bad);
+    status |= (int32_t)gor<BLK>(gm, bad);
     done = s + 1;
     if (p.history && p.record_every > 0 && (s + 1) % p.record_every == 0) {
       double* row = p.history + ((s + 1) / p.record_every - 1) * (b.nq_total + b.nv_total);
@@ -647,7 +725,27 @@ __global__ void __launch_bounds__(128) group_kernel(DeviceBatch b, StepParams p)
     if (w >= nwork) break;
     const int pk = b.active ? b.active[w / G] : w / G;
     const int l = (w % G) * P + gi;
-    if (l < b.packs[pk].count) grp::run_instance<S>(b, p, pk, l, G, t, gm, sm);
+    if (l < b.packs[pk].count) grp::run_instance<S, false>(b, p, pk, l, G, t, gm, sm);
     __syncwarp();
+  }
+}
+
+// The same step with a 4-warp block per instance (lanes per instance 128, one
+// body per thread): each block takes one instance at a time from the device
+// counter.  Dynamic shared memory: smem_words(nvp) + BLK_SCAN_WORDS doubles.
+__global__ void __launch_bounds__(128) group_block_kernel(DeviceBatch b, StepParams p) {
+  extern __shared__ double gsm[];
+  __shared__ int s_w;
+  const int t = threadIdx.x;
+  const int64_t nwork = (int64_t)(b.active ? b.nactive : b.npacks) * LANES;
+  while (true) {
+    if (t == 0) s_w = atomicAdd(b.queue, 1);
+    __syncthreads();
+    const int w = s_w;
+    __syncthreads();  // every thread has read s_w before thread 0 writes it again
+    if (w >= nwork) break;
+    const int pk = b.active ? b.active[w / LANES] : w / LANES;
+    const int l = w % LANES;
+    if (l < b.packs[pk].count) grp::run_instance<1, true>(b, p, pk, l, 32 * grp::BLK_WARPS, t, 0xffffffffu, gsm);
   }
 }

@@ -422,7 +422,9 @@ static int32_t coop_packs(const gpb_batch* b, int precision) {
 // Bodies per lane of the body-parallel mapping with `lanes` lanes per
 // instance, 0 if the batch cannot run it that way.
 static int group_bodies_per_lane(const gpb_batch* b, int lanes) {
-  if (!b->group_ok || lanes < 2 || lanes > LANES || (lanes & (lanes - 1))) return 0;
+  if (!b->group_ok) return 0;
+  if (lanes == 4 * LANES) return 1;  // a 4-warp block per instance: one body per thread
+  if (lanes < 2 || lanes > LANES || (lanes & (lanes - 1))) return 0;
   const int s = (b->nb_max + lanes - 1) / lanes;
   return s <= 1 ? 1 : (s == 2 ? 2 : 0);
 }
@@ -433,9 +435,9 @@ extern "C" int gpb_batch_set_mapping(gpb_batch* b, int lanes_per_instance) {
     if (!b->group_ok)
       return fail(GPB_E_INVAL, "gpb_batch_set_mapping: several lanes per instance need a batch of serial chains "
                                "of revolute, prismatic and fixed joints without cuboid colliders");
-    return fail(GPB_E_INVAL, "gpb_batch_set_mapping: lanes_per_instance must be 1 or a power of two in [2, 32] "
+    return fail(GPB_E_INVAL, "gpb_batch_set_mapping: lanes_per_instance must be 1, a power of two in [2, 32] "
                              "with at most two bodies per lane (this batch has chains of " +
-                                 std::to_string(b->nb_max) + " bodies)");
+                                 std::to_string(b->nb_max) + " bodies), or 128 (a 4-warp block per instance)");
   }
   b->lanes = lanes_per_instance;
   return GPB_OK;
@@ -689,10 +691,13 @@ extern "C" int gpb_batch_autotune(gpb_batch* b, double dt, int integrator, int p
         b->packs_h[0].minnv >= 32)
       for (int c : {40, 32}) cand.push_back({w, c, 1});
   }
-  // body-parallel chains: the group sizes with one or two bodies per lane
-  if ((precision == GPB_FP64 || precision == GPB_MIXED) && integrator != GPB_VELOCITY_STEPPING)
+  // body-parallel chains: the group sizes with one or two bodies per lane, and
+  // a 4-warp block per instance for chains longer than 16 bodies
+  if ((precision == GPB_FP64 || precision == GPB_MIXED) && integrator != GPB_VELOCITY_STEPPING) {
     for (int l = 2; l <= LANES; l *= 2)
       if (group_bodies_per_lane(b, l) && (l < 2 * b->nb_max || l == 2)) cand.push_back({0, 0, l});
+    if (group_bodies_per_lane(b, 4 * LANES) && b->nb_max > LANES / 2) cand.push_back({0, 0, 4 * LANES});
+  }
   double best = 1e300;
   Shape pick{keep_w, keep_c, keep_l};
   int err = GPB_OK;

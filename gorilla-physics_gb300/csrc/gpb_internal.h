@@ -243,8 +243,8 @@ struct StepParams {
 cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p,
                             int num_sms, int warps_per_sm, cudaStream_t s);
 // Body-parallel mapping of serial chains (gpb_group.cuh): p.group lanes per
-// instance, bodies_per_lane = 1 or 2 (p.group · bodies_per_lane ≥ every
-// instance's body count), FP64.
+// instance (2 … 32 lanes of a warp, or 128: a 4-warp block), bodies_per_lane
+// = 1 or 2 (p.group · bodies_per_lane ≥ every instance's body count), FP64.
 cudaError_t launch_simulate_group(const DeviceBatch& b, const StepParams& p, int bodies_per_lane, int num_sms,
                                   cudaStream_t s);
 cudaError_t launch_dynamics(const DeviceBatch& b, const StepParams& p, cudaStream_t s);

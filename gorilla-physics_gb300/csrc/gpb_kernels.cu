@@ -1409,23 +1409,26 @@ cudaError_t launch_simulate(const DeviceBatch& b, const StepParams& p, int num_s
 
 cudaError_t launch_simulate_group(const DeviceBatch& b, const StepParams& p, int bodies_per_lane, int num_sms,
                                   cudaStream_t s) {
-  if (p.group < 2 || p.group > LANES || (p.group & (p.group - 1)) || bodies_per_lane < 1 || bodies_per_lane > 2 ||
-      p.group_nvp < 0 || p.group_nvp > 2 * p.group)
+  const bool blk = p.group == 32 * grp::BLK_WARPS;  // a 4-warp block per instance
+  if (!(blk || (p.group >= 2 && p.group <= LANES && !(p.group & (p.group - 1)))) || bodies_per_lane < 1 ||
+      bodies_per_lane > (blk ? 1 : 2) || p.group_nvp < 0 || p.group_nvp > 2 * LANES)
     return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(b.queue, 0, 2 * sizeof(int32_t), s);
   if (e != cudaSuccess) return e;
   const int threads = 128;
-  const size_t smem = (size_t)(threads / 32) * (LANES / p.group) * grp::smem_words(p.group_nvp) * sizeof(double);
-  auto kern = bodies_per_lane == 1 ? group_kernel<1> : group_kernel<2>;
+  const size_t smem = blk ? (size_t)(grp::smem_words(p.group_nvp) + grp::BLK_SCAN_WORDS) * sizeof(double)
+                          : (size_t)(threads / 32) * (LANES / p.group) * grp::smem_words(p.group_nvp) * sizeof(double);
+  auto kern = blk ? group_block_kernel : (bodies_per_lane == 1 ? group_kernel<1> : group_kernel<2>);
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  const int64_t items = (int64_t)(b.active ? b.nactive : b.npacks) * p.group;
+  // work items: a pack's 32 / group instances per warp, or one instance per block
+  const int64_t items = (int64_t)(b.active ? b.nactive : b.npacks) * (blk ? LANES : p.group);
   int64_t grid = (int64_t)num_sms * per_sm;
-  const int64_t want = (items + (threads / 32) - 1) / (threads / 32);
+  const int64_t want = blk ? items : (items + (threads / 32) - 1) / (threads / 32);
   if (grid > want) grid = want;
   if (grid < 1) grid = 1;
   kern<<<(unsigned)grid, threads, smem, s>>>(b, p);

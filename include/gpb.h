@@ -351,7 +351,9 @@ int gpb_synchronize(gpb_ctx* ctx);
  * default);
  * 2, 4, 8, 16 or 32 = the body-parallel mapping, where that many lanes of a
  * warp step one instance (32 = one warp per instance, 2 = sixteen instances
- * per warp), each lane owning one or two consecutive bodies: the outward and
+ * per warp), each lane owning one or two consecutive bodies; 128 = the same
+ * with a 4-warp block per instance (one body per thread, the warps' scan
+ * totals combined in shared memory, a block barrier per Cholesky column): the outward and
  * inward sweeps are prefix and suffix scans across the lanes by warp
  * shuffles, and the mass matrix and its Cholesky factor sit in shared memory
  * with their entries dealt to the lanes.  It shortens one instance's step by

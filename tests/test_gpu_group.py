@@ -91,8 +91,9 @@ def random_chains(rng, n, nb_lo, nb_hi, contacts=False):
 
 
 def lane_counts(nb_max):
-    """The lane counts the mapping accepts: one or two bodies per lane."""
-    return [g for g in (2, 4, 8, 16, 32) if 2 * g >= nb_max]
+    """The lane counts the mapping accepts: one or two bodies per lane of a
+    warp, or a 4-warp block per instance (128)."""
+    return [g for g in (2, 4, 8, 16, 32) if 2 * g >= nb_max] + [128]
 
 
 def state(rng, M, qscale=math.pi):
@@ -138,11 +139,11 @@ def test_one_step_against_oracle(ctx, nb_lo, nb_hi, integrator):
         assert rel_err(q, q1) < 1e-10 and rel_err(v, v1) < 1e-10, g
 
 
-@pytest.mark.parametrize("control", ["host", "open_loop", "pd"])
-def test_trajectory_200_steps(ctx, control):
+@pytest.mark.parametrize("control,lanes", [("host", 32), ("open_loop", 32), ("pd", 32), ("open_loop", 128)])
+def test_trajectory_200_steps(ctx, control, lanes):
     """200 steps of C1 chains (2–48 DOF) with each control law, one warp per
-    instance and two bodies per lane where needed: final state and the
-    recorded history against the oracle (1e-8)."""
+    instance (two bodies per lane where needed) or a block per instance: final
+    state and the recorded history against the oracle (1e-8)."""
     n = 64
     M, q0, v0, aux = Model.from_config(1, n, seed=31)
     qo, vo, _ = M.offsets()
@@ -150,7 +151,7 @@ def test_trajectory_200_steps(ctx, control):
     kw = dict(seed=77, resample_every=10, sigma=1.0, kp=50.0, kd=2.0)
     ctl = aux if control == "pd" else None
     B = Batch(M, ctx)
-    B.set_mapping(32)
+    B.set_mapping(lanes)
     B.update(q0, v0)
     hist = B.simulate_steps(200, dt, gpb.SEMI_IMPLICIT_EULER, gpb.FP64, control, tau=ctl, record_every=50, **kw)
     q, v = B.state()
@@ -208,7 +209,7 @@ def test_failures_are_flagged_and_frozen(ctx):
     q0[qo[5]] = np.nan
     jo = M.joint_offset
     M.body_inertia[10 * jo[9]:10 * jo[10]] *= -1.0  # instance 9: every inertia negative
-    for g in (1, 16, 32):
+    for g in (1, 16, 32, 128):
         if g > 1 and 2 * g < int(np.max(np.diff(jo))):
             continue
         B = Batch(M, ctx)
@@ -234,7 +235,7 @@ def test_mapping_rules(ctx):
     M, q0, v0, _ = Model.from_config(1, 40, seed=6)  # up to 48 bodies: only 32 lanes give ≤ 2 per lane
     nb_max = int(np.max(np.diff(M.joint_offset)))
     B = Batch(M, ctx)
-    for bad in (0, 3, 64):
+    for bad in (0, 3, 64, 256):
         with pytest.raises(gpb.GpbError):
             B.set_mapping(bad)
     if nb_max > 32:
@@ -291,7 +292,7 @@ def test_autotune_chooses_among_mappings(ctx):
     B = Batch(M, ctx)
     B.update(q0, v0)
     w, c, lanes = B.autotune(5e-4, gpb.SEMI_IMPLICIT_EULER, gpb.FP64, trial_steps=5)
-    assert lanes in (1, 32) and (lanes > 1 or w in (4, 8, 12, 16))
+    assert lanes in (1, 32, 128) and (lanes > 1 or w in (4, 8, 12, 16))
     q1, v1 = B.state()
     assert np.array_equal(q1, q0) and np.array_equal(v1, v0)
     B.simulate_steps(100, 5e-4)
