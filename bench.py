@@ -1064,6 +1064,7 @@ def run_cuboids(args):
                 "d2h_bytes_per_step": (qo.nbytes + vo.nbytes) / args.steps,
                 "note": "gpb_set_state (pinned host) + gpb_simulate + gpb_get_state"},
     }
+    line["kernel_source_sha16"] = kernel_source_hash()
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_cuboids(M, q0, v0, args.steps)
     if rank == 0:
@@ -1201,6 +1202,7 @@ def run_vstep(args):
         line["cpu_baseline"] = {"value": sample * K / el, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"first {sample} of {n} cubes x {K} steps (oracle restatement, "
                                           f"{threads} host threads)"}
+    line["kernel_source_sha16"] = kernel_source_hash()
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -33,6 +33,34 @@ def test_committed_headline_line():
             assert m["value"] <= d["value"] * (1 + 1e-12), name
 
 
+def test_committed_lines_record_their_mapping():
+    """Every committed bench line records each form's launch shape; where the
+    autotuner chose several lanes per instance, the line carries the one-lane
+    run it was compared with and the chosen shape was the faster; the small
+    batches of chains pick the body-parallel mapping."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    picked = {}
+    for f in sorted((ROOT / "profiles").glob("bench_*.json")):
+        d = json.loads(f.read_text().strip().splitlines()[-1])
+        if not d["config"]["workload"].split(" x ")[0] in bench.CONFIG_NAME.values():
+            continue  # the cuboid-collider and velocity-stepping benchmarks have no mapping choice
+        for name, m in d["modes"].items():
+            launch = m["launch"]
+            assert {"warps_per_sm", "coop_min_dof", "lanes_per_instance"} <= set(launch), (f.name, name)
+            lanes = launch["lanes_per_instance"]
+            assert lanes in (1, 2, 4, 8, 16, 32, 128), (f.name, name)
+            if lanes > 1:
+                assert m["value"] >= launch["one_lane"]["value"], (f.name, name)
+                assert "body-parallel" in m["algorithm"], (f.name, name)
+            picked[(f.name, name)] = lanes
+        assert d.get("kernel_source_sha16") == bench.kernel_source_hash(), f.name
+    assert picked[("bench_serial-chain_1024.json", "fp64_crba")] > 1
+    assert picked[("bench_serial-chain_256.json", "fp64_crba")] > 1
+    assert picked[("bench_serial-chain_65536.json", "mixed")] == 1
+
+
 def test_ncu_tables_hold_what_bench_reads():
     t = json.loads((ROOT / "profiles" / "dram_traffic_per_instance_step.json").read_text())
     m = t["serial-chain"]["mixed"]
