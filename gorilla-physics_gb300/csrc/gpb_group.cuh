@@ -21,9 +21,11 @@
 //             H_ij = (Ic_i S_i) · S_j for j ≤ i (src/mechanism.rs:592-696);
 //             the lower triangle is filled in shared memory, its entries dealt
 //             evenly to the lanes;
-//   solve     Cholesky H = L Lᵀ, right-looking, each column's trailing update
-//             dealt evenly to the lanes, then the two triangular solves
-//             (src/dynamics.rs:255-276 solves the same system by LU).
+//   solve     Cholesky H = L Lᵀ, right-looking by 4-column panels (every lane
+//             factors the diagonal block, the rows below it and the trailing
+//             update's entries are dealt evenly to the lanes), then the two
+//             triangular solves by the same panels (src/dynamics.rs:255-276
+//             solves the same system by LU).
 // It serves instances too few to fill the GPU one lane each, where the
 // latency of one instance's step sets the rate.  The arithmetic is FP64 for
 // GPB_FP64 and GPB_MIXED requests alike: a double-float version of this
@@ -204,7 +206,11 @@ __device__ __forceinline__ IFc excl_suffix(IFc x, int t, int G, unsigned gm, con
 // triangle of H (row i at i(i+1)/2), the world motion subspaces and the
 // columns Ic_i S_i (6 n each, component-major), the right-hand side, the
 // intermediate vector of the solves and the reciprocal pivots (n each).
-__host__ __device__ inline int smem_words(int n) { return n * (n + 1) / 2 + 15 * n; }
+// The matrix is padded to whole 4×4 panels (identity rows beyond n).
+__host__ __device__ inline int smem_words(int n) {
+  const int m = (n + 3) & ~3;
+  return m * (m + 1) / 2 + 15 * m;
+}
 // A block per instance also keeps its warps' scan totals: 4 warps × 16 doubles.
 constexpr int BLK_WARPS = 4;
 constexpr int BLK_SCAN_WORDS = BLK_WARPS * 16;
@@ -417,7 +423,7 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
     }
   }
   // ---- right-hand side, columns Ic S, diagonal of H
-  const int n = g.nv, np = g.nvp;
+  const int n = g.nv, np = (g.nvp + 3) & ~3, n4 = (n + 3) & ~3;
   double* H = g.sm;
   double* Ssm = H + off(np);
   double* Fsm = Ssm + 6 * np;
@@ -463,32 +469,80 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
       }
     }
   }
-  // ---- Cholesky H = L Lᵀ in place (right-looking)
+  // padding rows n … n4−1: identity rows, zero right-hand side
+  for (int i = n; i < n4; ++i) {
+    for (int j = t; j <= i; j += G) H[off(i) + j] = j == i ? 1.0 : 0.0;
+    if (t == 0) x[i] = 0.0;
+  }
+  // ---- Cholesky H = L Lᵀ in place, right-looking by 4-column panels: every
+  // lane factors the 4×4 diagonal block in registers, the rows below it are
+  // dealt to the lanes (each a 4-term triangular solve), then the trailing
+  // block takes a rank-4 update entry by entry — two barriers per panel
   int st = 0;
-  for (int k = 0; k < n; ++k) {
+  for (int k = 0; k < n4; k += 4) {
     gsync<BLK>(gm);
-    double d = H[off(k) + k];
-    if (!(d > 0.0)) {
-      st |= 2;  // GPB_ST_CHOL_FAIL; continue with a unit pivot, as the one-lane factor does
-      d = 1.0;
+    double L[4][4], r[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int c = 0; c <= a; ++c) L[a][c] = H[off(k + a) + k + c];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      double d = L[c][c];
+#pragma unroll
+      for (int e = 0; e < c; ++e) d = fma(-L[c][e], L[c][e], d);
+      if (!(d > 0.0)) {
+        st |= 2;  // GPB_ST_CHOL_FAIL; continue with a unit pivot, as the one-lane factor does
+        d = 1.0;
+      }
+      r[c] = rsqrt(d);
+      L[c][c] = d * r[c];
+#pragma unroll
+      for (int a = c + 1; a < 4; ++a) {
+        double v = L[a][c];
+#pragma unroll
+        for (int e = 0; e < c; ++e) v = fma(-L[a][e], L[c][e], v);
+        L[a][c] = v * r[c];
+      }
     }
-    const double r = rsqrt(d);
-    for (int i = k + 1 + t; i < n; i += G) H[off(i) + k] *= r;
+    for (int i = k + 4 + t; i < n4; i += G) {  // the panel's rows below the block
+      double l[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        double v = H[off(i) + k + c];
+#pragma unroll
+        for (int e = 0; e < c; ++e) v = fma(-l[e], L[c][e], v);
+        l[c] = v * r[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) H[off(i) + k + c] = l[c];
+    }
     gsync<BLK>(gm);
-    if (t == 0) {  // every lane has read the pivot: the barrier above orders this write after them
-      H[off(k) + k] = d * r;
-      dinv[k] = r;
+    if (t == 0) {  // the block's factor: no lane reads the block again in this panel
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+#pragma unroll
+        for (int c = 0; c <= a; ++c) H[off(k + a) + k + c] = L[a][c];
+        dinv[k + a] = r[a];
+      }
     }
-    // trailing block rows k+1 … n−1, entry (a, c), c ≤ a, to lane (a(a+1)/2 + c) mod G
-    const int m = n - k - 1;
+    // trailing block rows k+4 … n4−1, entry (a, c), c ≤ a, to lane (a(a+1)/2 + c) mod G
+    const int m = n4 - k - 4;
     int a = 0, c = t;
     while (c > a) {
       c -= a + 1;
       ++a;
     }
     while (a < m) {
-      const int i = k + 1 + a, j = k + 1 + c;
-      H[off(i) + j] = fma(-H[off(i) + k], H[off(j) + k], H[off(i) + j]);
+      const int i = k + 4 + a, j = k + 4 + c;
+      const double* li = H + off(i) + k;
+      const double* lj = H + off(j) + k;
+      double h = H[off(i) + j];
+      h = fma(-li[0], lj[0], h);
+      h = fma(-li[1], lj[1], h);
+      h = fma(-li[2], lj[2], h);
+      h = fma(-li[3], lj[3], h);
+      H[off(i) + j] = h;
       c += G;
       while (c > a) {
         c -= a + 1;
@@ -496,18 +550,44 @@ __device__ __noinline__ int eval(const Inst<S>& gin, const double (&qin)[S], con
       }
     }
   }
-  // ---- L y = rhs (y into z), then Lᵀ q̈ = y (into x)
-  for (int k = 0; k < n; ++k) {
+  // ---- L y = rhs (y into z), then Lᵀ q̈ = y (into x), by the same panels:
+  // every lane solves the 4×4 block, the other rows are dealt to the lanes
+  for (int k = 0; k < n4; k += 4) {
     gsync<BLK>(gm);
-    const double y = x[k] * dinv[k];
-    for (int i = k + 1 + t; i < n; i += G) x[i] = fma(-H[off(i) + k], y, x[i]);
-    if (t == 0) z[k] = y;
+    double y[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      double v = x[k + a];
+#pragma unroll
+      for (int e = 0; e < a; ++e) v = fma(-H[off(k + a) + k + e], y[e], v);
+      y[a] = v * dinv[k + a];
+    }
+    for (int i = k + 4 + t; i < n4; i += G) {
+      const double* li = H + off(i) + k;
+      x[i] = fma(-li[3], y[3], fma(-li[2], y[2], fma(-li[1], y[1], fma(-li[0], y[0], x[i]))));
+    }
+    if (t == 0) {
+#pragma unroll
+      for (int a = 0; a < 4; ++a) z[k + a] = y[a];
+    }
   }
-  for (int k = n - 1; k >= 0; --k) {
+  for (int k = n4 - 4; k >= 0; k -= 4) {
     gsync<BLK>(gm);
-    const double xk = z[k] * dinv[k];
-    for (int i = t; i < k; i += G) z[i] = fma(-H[off(k) + i], xk, z[i]);
-    if (t == 0) x[k] = xk;
+    double w[4];
+#pragma unroll
+    for (int a = 3; a >= 0; --a) {
+      double v = z[k + a];
+#pragma unroll
+      for (int e = a + 1; e < 4; ++e) v = fma(-H[off(k + e) + k + a], w[e], v);
+      w[a] = v * dinv[k + a];
+    }
+    for (int i = t; i < k; i += G)
+      z[i] = fma(-H[off(k + 3) + i], w[3],
+                 fma(-H[off(k + 2) + i], w[2], fma(-H[off(k + 1) + i], w[1], fma(-H[off(k) + i], w[0], z[i]))));
+    if (t == 0) {
+#pragma unroll
+      for (int a = 0; a < 4; ++a) x[k + a] = w[a];
+    }
   }
   gsync<BLK>(gm);
 #pragma unroll
