@@ -2,9 +2,11 @@
 // gpb_kernels.cu after the per-lane evaluators, make_ctx and control).
 //
 // G lanes of a warp (G = 2, 4, 8, 16 or 32) step one instance together, so a
-// warp holds 32 / G instances of a pack; G = 32 is one warp per instance.
-// Lane t of a group owns the S consecutive bodies t·S … t·S + S − 1 of the
-// chain (S = 1 or 2, G·S ≥ bodies).  One dynamics evaluation
+// warp holds 32 / G instances of a pack; G = 32 is one warp per instance; or a
+// whole 4-warp block does (G = 128, group_block_kernel: the warps' scan totals
+// meet in shared memory and the barriers are block barriers).  Lane t of a
+// group owns the S consecutive bodies t·S … t·S + S − 1 of the chain (S = 1 or
+// 2, G·S ≥ bodies).  One dynamics evaluation
 // (src/dynamics.rs:322-364) becomes:
 //   outward   world poses are the prefix products X_1 X_2 … X_b of the joint
 //             transforms; body velocities and bias accelerations are prefix
