@@ -675,9 +675,65 @@ __device__ __forceinline__ void solve6(const double* L, const double* dinv, doub
   }
 }
 
+// The same factor and solve in double-float (the mixed form's floating
+// joints): each pivot's 1/√x by ff_rsqrt after renormalising x, whose sign
+// the test reads from hi.
+__device__ __forceinline__ bool chol6_ff(const ABIF& I, FF* L, FF* dinv) {
+  FF M6[21];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      FF x;
+      if (i < 3) x = symget(I.A, i, j);
+      else if (j < 3) x = I.B[3 * j + (i - 3)];  // block (v, ω) = Bᵀ
+      else x = symget(I.C, i - 3, j - 3);
+      M6[l6(i, j)] = x;
+    }
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      FF x = M6[l6(i, j)];
+#pragma unroll
+      for (int k = 0; k < j; ++k) x = ff_fms(x, L[l6(i, k)], L[l6(j, k)]);
+      if (i == j) {
+        x = two_sum(x.hi, x.lo);
+        if (!(x.hi > 0.0f)) {
+          ok = false;
+          x = ff(1.0f);
+        }
+        dinv[i] = ff_rsqrt(x);
+        L[l6(i, i)] = ff_mul(x, dinv[i]);
+      } else {
+        L[l6(i, j)] = ff_mul(x, dinv[j]);
+      }
+    }
+  }
+  return ok;
+}
+__device__ __forceinline__ void solve6_ff(const FF* L, const FF* dinv, FF* x) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    FF s = x[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) s = ff_fms(s, L[l6(i, k)], x[k]);
+    x[i] = ff_mul(s, dinv[i]);
+  }
+#pragma unroll
+  for (int i = 5; i >= 0; --i) {
+    FF s = x[i];
+#pragma unroll
+    for (int k = i + 1; k < 6; ++k) s = ff_fms(s, L[l6(k, i)], x[k]);
+    x[i] = ff_mul(s, dinv[i]);
+  }
+}
+
 // Per-DOF record of the inward pass (DU region, 11 words per DOF):
 //   1-DOF joint: U (6), 1/D, u
-//   floating joint (its 6 DOF slots, 66 words): L (21), 1/diag (6), u (6)
+//   floating joint (its 6 DOF slots, 66 words): L (21), 1/diag (6), u (6) —
+//   FP64 words in the FP64 form, FF words in the mixed form
 constexpr int DU_D = 11;
 
 // I·(w, v) in the sweep precision R (the bias-force update needs only R).
@@ -930,22 +986,21 @@ __device__ __forceinline__ int aba_inward_ff(const LaneCtx<R>& c, Col<double> q,
           pa.v[i] = ff_add(pA.v[i], ff_fma(Uv[i], ud, ff(iv[i])));
         }
       }
-    } else if (type == 3) {  // floating joint: the FP64 6×6 solve of the FP64 form
-      double L[21], dinv[6];
-      if (!chol6(abi_to_double(IA), L, dinv)) st |= 2;
+    } else if (type == 3) {  // floating joint: the 6×6 factor of the FP64 form, in double-float
+      FF L[21], dinv[6];
+      if (!chol6_ff(IA, L, dinv)) st |= 2;
       const int du = c.L.DU + DU_D * vo;
 #pragma unroll
-      for (int k = 0; k < 21; ++k) c.d(du + k) = L[k];
+      for (int k = 0; k < 21; ++k) ffw(c, du + k) = L[k];
 #pragma unroll
-      for (int k = 0; k < 6; ++k) c.d(du + 21 + k) = dinv[k];
+      for (int k = 0; k < 6; ++k) ffw(c, du + 21 + k) = dinv[k];
       const FF p6[6] = {pA.w[0], pA.w[1], pA.w[2], pA.v[0], pA.v[1], pA.v[2]};
       FF pa6[6];
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
-        const double pv = ff_to_double(p6[k]);
-        const double u = (have_tau ? tau[vo + k] : 0.0) - pv;
-        c.d(du + 27 + k) = u;
-        pa6[k] = ff_from_double(pv + u);  // floating joint: I^a = 0, p^a = p^A + u
+        const FF u = have_tau ? ff_sub(ff_from_double(tau[vo + k]), p6[k]) : ff_neg(p6[k]);
+        ffw(c, du + 27 + k) = u;
+        pa6[k] = ff_add(p6[k], u);  // floating joint: I^a = 0, p^a = p^A + u
       }
       pa = {{pa6[0], pa6[1], pa6[2]}, {pa6[3], pa6[4], pa6[5]}};
     } else {  // fixed joint: I^a = I^A, p^a = p^A + I^A c
@@ -1134,8 +1189,10 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     // velocity: v = X v_p + S q̇ ; bias acceleration c = v ×m (S q̇)
     V jw = zero, jv = zero;
     if (dvel) {  // FP64 recursion, rounded for the FP32 bias terms
-      vld = mulT(Rd, vld + cross(omd, td));
-      omd = mulT(Rd, omd);
+      if (parent != 0) {  // a body on the world starts from rest
+        vld = mulT(Rd, vld + cross(omd, td));
+        omd = mulT(Rd, omd);
+      }
       VD jwd{0.0, 0.0, 0.0}, jvd{0.0, 0.0, 0.0};
       if (type == 1 || type == 2) {
         const VD axd{c.td(tb + TD_AXIS), c.td(tb + TD_AXIS + 1), c.td(tb + TD_AXIS + 2)};
@@ -1152,8 +1209,10 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       jw = {R(jwd.x), R(jwd.y), R(jwd.z)};
       jv = {R(jvd.x), R(jvd.y), R(jvd.z)};
     } else {
-      vl = mulT(Rr, vl + cross(om, t));
-      om = mulT(Rr, om);
+      if (!(contacts && parent == 0)) {
+        vl = mulT(Rr, vl + cross(om, t));
+        om = mulT(Rr, om);
+      }
       if (type == 1 || type == 2) {
         const V ax{c.t(tb + TD_AXIS), c.t(tb + TD_AXIS + 1), c.t(tb + TD_AXIS + 2)};
         if (type == 1) jw = ax * R(v[vo]);
@@ -1182,17 +1241,38 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
     // of the bias force, and the root's u = τ − p^A reads it directly
     SV<double> wc{{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
     if (contacts) {
-      posw = posw + mul(Rw, td);
-      Rw = mul(Rw, Rd);
+      if (parent == 0) {  // a body on the world: its joint transform is its world pose
+        posw = td;
+        Rw = Rd;
+      } else {
+        posw = posw + mul(Rw, td);
+        Rw = mul(Rw, Rd);
+      }
       const int cb0 = (w1 >> 8) & 255, cn = (w1 >> 16) & 255;
       if (cn) {
-        // Only the penetration needs FP64 (it is a small difference of O(1)
-        // positions, and k·δ becomes force); the force law, the contact
-        // velocity and the wrench run in R in the body frame (the law depends
-        // only on n·v, |v_t| and z, so it is frame-independent).
+        // Poses and penetrations in FP64 (a penetration is a small difference
+        // of O(1) positions, and k·δ becomes force), and so are the
+        // contact-point velocity v + ω × r (it cancels for rolling or sticking
+        // contacts) and its split into the approach speed ż = −v·n and the
+        // tangential part v_t = v + n ż (which cancels for normal impacts, and
+        // which the regularised friction divides by 1e-3).  The FP64 form
+        // runs the force law and the wrench in FP64 too; the mixed form runs
+        // them in FP32 from those FP64 differences (the law depends only on z,
+        // ż and v_t), in the body frame.
         M3<R> RwR;
 #pragma unroll
         for (int k = 0; k < 9; ++k) RwR.a[k] = R(Rw.a[k]);
+        V ww = zero, wv = zero;  // the mixed form's wrench
+        // the mixed form forms the first half-space's normal in the body frame
+        // and the body origin's signed distance once per body: a point's
+        // penetration is then one dot product
+        VD nb0{0.0, 0.0, 0.0};
+        double d00 = 0.0;
+        if (sizeof(R) == 4 && c.nh > 0) {
+          const VD hn0{c.hdd(3), c.hdd(4), c.hdd(5)};
+          nb0 = mulT(Rw, hn0);
+          d00 = dot(posw - VD{c.hdd(0), c.hdd(1), c.hdd(2)}, hn0);
+        }
         for (int k = cb0; k < cb0 + cn; ++k) {
           const int cd = CTC_D * k;
           const VD locd{c.cdd(cd), c.cdd(cd + 1), c.cdd(cd + 2)};
@@ -1200,13 +1280,15 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
           const R kp = c.CD[(size_t)(cd + 3) * LANES], rad = c.CD[(size_t)(cd + 4) * LANES],
                   damp = c.CD[(size_t)(cd + 5) * LANES];
           const double radd = c.cdd(cd + 4);
-          const VD pwc = mul(Rw, locd) + posw;
+          const VD pwc = sizeof(R) == 8 ? mul(Rw, locd) + posw : VD{0.0, 0.0, 0.0};
           V fsum = zero;
           for (int h = 0; h < c.nh; ++h) {
             const int hd = HS_D * h;
             const VD hp{c.hdd(hd), c.hdd(hd + 1), c.hdd(hd + 2)};
             const VD hnd{c.hdd(hd + 3), c.hdd(hd + 4), c.hdd(hd + 5)};
-            const double dist = dot(pwc - hp, hnd);
+            const bool first = sizeof(R) == 4 && h == 0;
+            const double dist = first ? d00 + dot(nb0, locd)
+                                      : dot((sizeof(R) == 8 ? pwc : mul(Rw, locd) + posw) - hp, hnd);
             double pen;
             if (radd > 0.0) {
               if (!(dist - radd <= 1e-8)) continue;
@@ -1216,11 +1298,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
               pen = -dist;
             }
             const double alh = c.hdd(hd + 6), mu = c.hdd(hd + 7);
-            // The contact-point velocity v + ω × r cancels for rolling or
-            // sticking contacts, its tangential part cancels for normal impacts,
-            // and the regularised friction divides it by 1e-3: the velocity and
-            // the force law run in FP64, the wrench in R.
-            const VD nbd = mulT(Rw, hnd);  // normal in the body frame
+            const VD nbd = first ? nb0 : mulT(Rw, hnd);  // normal in the body frame
             const V nb{R(nbd.x), R(nbd.y), R(nbd.z)};
             const V app = rad > R(0) ? loc - nb * rad : loc;  // application point (body frame)
             const VD appd = radd > 0.0 ? locd - nbd * radd : locd;
@@ -1232,10 +1310,20 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
             const VD omc = root6 ? VD{v[vo], v[vo + 1], v[vo + 2]}
                                  : (dvel ? omd : VD{double(om.x), double(om.y), double(om.z)});
             const VD vd = vlc + cross(omc, appd);
-            const VD fbd = contact_force<double>(c.model, pen, nbd, vd, c.cdd(cd + 3), c.cdd(cd + 5), alh, mu);
-            const V fb{R(fbd.x), R(fbd.y), R(fbd.z)};
-            wc.w = wc.w - cross(appd, fbd);
-            wc.v = wc.v - fbd;
+            V fb;
+            if (sizeof(R) == 4) {
+              const double zd = -dot(vd, nbd);
+              const VD vtd = vd + nbd * zd;
+              fb = contact_force_parts<R>(c.model, R(pen), R(zd), nb, V{R(vtd.x), R(vtd.y), R(vtd.z)}, kp, damp,
+                                          R(alh), R(mu));
+              ww = ww - cross(app, fb);
+              wv = wv - fb;
+            } else {
+              const VD fbd = contact_force<double>(c.model, pen, nbd, vd, c.cdd(cd + 3), c.cdd(cd + 5), alh, mu);
+              fb = V{R(fbd.x), R(fbd.y), R(fbd.z)};
+              wc.w = wc.w - cross(appd, fbd);
+              wc.v = wc.v - fbd;
+            }
             fsum = fsum + fb;
           }
           if (want_cf) {
@@ -1246,6 +1334,7 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
             cf[3 * orig + 2] = double(fw.z);
           }
         }
+        if (sizeof(R) == 4) wc = {{double(ww.x), double(ww.y), double(ww.z)}, {double(wv.x), double(wv.y), double(wv.z)}};
       }
       const int uslot = (int)((w1 >> W1_CUBOID_SHIFT) & 15u);
       if (uslot && c.nu > 1) {  // cuboid record: world pose, world twist about the origin
@@ -1567,6 +1656,23 @@ __device__ __noinline__ int lane_aba(const LaneCtx<R>& cin, Col<double> q, Col<d
       if (!isfinite(x)) st |= 1;  // GPB_ST_NONFINITE
       if (type == 1) a.w = a.w + ax * xr;
       else a.v = a.v + ax * xr;
+    } else if (type == 3 && sizeof(R) == 4) {  // the mixed form's double-float record
+      FF x[6], L[21], dinv[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) x[k] = ffw(c, du + 27 + k);
+#pragma unroll
+      for (int k = 0; k < 21; ++k) L[k] = ffw(c, du + k);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) dinv[k] = ffw(c, du + 21 + k);
+      solve6_ff(L, dinv, x);
+      const float a6[6] = {float(a.w.x), float(a.w.y), float(a.w.z), float(a.v.x), float(a.v.y), float(a.v.z)};
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const double y = ff_to_double(ff_addf(x[k], -a6[k]));
+        qdd[vo + k] = y;
+        if (!isfinite(y)) st |= 1;
+      }
+      a = {{R(ff_f(x[0])), R(ff_f(x[1])), R(ff_f(x[2]))}, {R(ff_f(x[3])), R(ff_f(x[4])), R(ff_f(x[5]))}};
     } else if (type == 3) {
       // q̈ = D⁻¹ (u − Uᵀ a') with U = D = I^A, i.e. D⁻¹ u − a'; then a = D⁻¹ u
       double x[6];

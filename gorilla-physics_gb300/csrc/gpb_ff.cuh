@@ -139,6 +139,16 @@ __device__ __forceinline__ FF ff_rcp(FF d) {
   return fast_two_sum(r, __fmul_rn(r, res));
 }
 
+// 1/√x for x > 0 (hi + lo normalised): the FP32 rsqrtf refined by one Newton
+// step, y + y·(1 − x·y²)/2, with the residual 1 − x·y² formed from the exact
+// square y² and an FF product.  rsqrtf's relative error δ (a few 2^-24) leaves
+// 3δ²/2 after the step, below 1e-13.
+__device__ __forceinline__ FF ff_rsqrt(FF x) {
+  const float y = rsqrtf(x.hi);
+  const FF r = ff_sub(ff(1.0f), ff_mul(x, two_prod(y, y)));
+  return fast_two_sum(y, __fmul_rn(__fmul_rn(0.5f, y), ff_f(r)));
+}
+
 // Conversions (FP64 instructions: keep them out of inner loops).
 __device__ __forceinline__ FF ff_from_double(double x) {
   const float hi = __double2float_rn(x);

@@ -174,11 +174,11 @@ __device__ __forceinline__ void sincos_q<float>(double q, float* s, float* c) {
 }
 
 // Contact force of one point against one half-space (src/contact.rs:260-338),
-// or the linear spring–damper law.
+// or the linear spring–damper law, from the penetration z, the approach speed
+// ż = −v·n and the tangential velocity v_t = v + n ż of the contact point.
 template <typename R>
-__device__ __forceinline__ V3<R> contact_force(int model, R z, V3<R> n, V3<R> vel, R k_point,
-                                               R damping, R alpha, R mu) {
-  R zdot = -dot(vel, n);
+__device__ __forceinline__ V3<R> contact_force_parts(int model, R z, R zdot, V3<R> n, V3<R> vt, R k_point,
+                                                     R damping, R alpha, R mu) {
   R pi;
   if (model == 1) {
     pi = fmax(k_point * z + damping * zdot, R(0));
@@ -190,7 +190,6 @@ __device__ __forceinline__ V3<R> contact_force(int model, R z, V3<R> n, V3<R> ve
     pi = fmax(lam * zn * zdot + k * zn, R(0));
   }
   V3<R> f = n * pi;
-  V3<R> vt = vel + n * zdot;
   R vtn = sqrt(dot(vt, vt));
   if (vtn != R(0)) {
     R s = vtn / R(1e-3);
@@ -199,6 +198,13 @@ __device__ __forceinline__ V3<R> contact_force(int model, R z, V3<R> n, V3<R> ve
     f = f + vt * g;
   }
   return f;
+}
+// The same law from the contact point's velocity v.
+template <typename R>
+__device__ __forceinline__ V3<R> contact_force(int model, R z, V3<R> n, V3<R> vel, R k_point,
+                                               R damping, R alpha, R mu) {
+  const R zdot = -dot(vel, n);
+  return contact_force_parts<R>(model, z, zdot, n, vel + n * zdot, k_point, damping, alpha, mu);
 }
 
 // ---------------------------------------------------------------------------
