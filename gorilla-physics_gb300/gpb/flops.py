@@ -76,21 +76,37 @@ def model_flops(model, integrator: int = 0) -> np.ndarray:
 #   other revolute 845, prismatic 800 (full 3×3 rotation of the congruence,
 #   Rodrigues, U = I^A S with a general axis), floating root 440 (6×6
 #   Cholesky and solve), fixed 650
-#   contact point 130, plus 60 per body of a mechanism with contacts (FP64
-#   world poses)
-# GPB_MIXED runs the articulated-inertia recursion and the 1-DOF q̈ solve in
-# double-float on the FP32 pipes; what stays FP64 is the state update, u, the
-# reduction of q before sin/cos, the open-loop torque draw, a floating root's
-# 6×6 Cholesky and everything that places contacts: 23 per planar revolute
-# body (ncu on 65,536 serial chains: 575 FP64 flops per instance-step), 50
-# other revolute (Rodrigues), 30 prismatic, 240 floating root, 10 fixed;
-# contacts as above.
+#   contact point 130, plus 60 per body of a mechanism with contacts whose
+#   parent is not the world (FP64 world poses; a body on the world takes its
+#   joint transform as its pose)
+# GPB_MIXED runs the articulated-inertia recursion, the 1-DOF q̈ solve and a
+# floating joint's 6×6 factor and solve in double-float on the FP32 pipes;
+# what stays FP64 is the state update, u, the reduction of q before sin/cos
+# and the open-loop torque draw: 23 per planar revolute body (ncu on 65,536
+# serial chains: 575 FP64 flops per instance-step), 50 other revolute
+# (Rodrigues), 30 prismatic, 10 fixed, and 165 per floating joint (its
+# quaternion to rotation 31, joint offset 18, FP64↔double-float conversions
+# of its bias force and q̈ 12, velocity sums 6, the quaternion and position
+# update 98).  A mechanism with contacts keeps in FP64 only the contact
+# differences that cancel:
+#   contact point 18 (penetration test 6; for a point in contact, 24 more for
+#   the contact-point velocity v + ω × r and its split into ż and v_t: half
+#   of the points in contact on average), plus 23 per body with points (the
+#   half-space's body-frame normal and the origin's signed distance);
+#   per body whose parent is not the world, 120 (FP64 world pose 63, FP64
+#   body-velocity recursion 51, FP64 joint rotation 6).
+# ncu on 32,768 cubes in flight (the first 20 steps, mostly before landing):
+# 284 FP64 flops per cube-step (96 DFMA, 46 DADD, 46 DMUL per cube); this
+# count gives 236 with no point in contact and 332 with half of them.
 # ---------------------------------------------------------------------------
 
 ABA_FP64 = {"rev_planar": 620, "rev": 845, "pri": 800, "float": 440, "fixed": 650}
-ABA_MIXED_FP64 = {"rev_planar": 23, "rev": 50, "pri": 30, "float": 240, "fixed": 10}
+ABA_MIXED_FP64 = {"rev_planar": 23, "rev": 50, "pri": 30, "float": 165, "fixed": 10}
 ABA_CONTACT = 130
 ABA_POSE = 60
+ABA_MIXED_CONTACT = 18
+ABA_MIXED_CONTACT_BODY = 23
+ABA_MIXED_POSE = 120
 
 
 def _aba_kinds(model, i):
@@ -115,16 +131,21 @@ def aba_model_flops(model, mixed: bool = False, integrator: int = 0) -> np.ndarr
     evals = {0: 1, 1: 2, 2: 4}[integrator]
     table = ABA_MIXED_FP64 if mixed else ABA_FP64
     out = np.zeros(model.n, np.int64)
-    co = model.contact_offset
+    co, jo, ho = model.contact_offset, model.joint_offset, model.halfspace_offset
     cache: dict = {}
     for i in range(model.n):
         kinds = tuple(_aba_kinds(model, i))
         nc = int(co[i + 1] - co[i])
-        key = (kinds, nc)
+        off_world = int(np.count_nonzero(model.joint_parent[jo[i]:jo[i + 1]]))
+        # bodies carrying points (contact_body is 1-based) × half-spaces
+        with_points = len(set(model.contact_body[co[i]:co[i + 1]].tolist())) * int(ho[i + 1] - ho[i])
+        key = (kinds, nc, off_world, with_points)
         if key not in cache:
             f = sum(table[k] for k in kinds)
-            if nc:
-                f += ABA_CONTACT * nc + ABA_POSE * len(kinds)
+            if nc and mixed:
+                f += ABA_MIXED_CONTACT * nc + ABA_MIXED_CONTACT_BODY * with_points + ABA_MIXED_POSE * off_world
+            elif nc:
+                f += ABA_CONTACT * nc + ABA_POSE * off_world
             cache[key] = f
         out[i] = evals * cache[key]
     return out
