@@ -106,9 +106,12 @@ enum gpb_precision { GPB_FP64 = 0, GPB_MIXED = 1, GPB_MIXED_REFINED = 2 };
  *   CRBA to the conditioning bound).  With GPB_MIXED its articulated-inertia
  *   recursion, the body bias forces v ×* I v with their inward recursion and
  *   the 1-DOF q̈ solve run in double-float (pairs of FP32 numbers, about 48
- *   bits, on the FP32 pipes) from the FP32-rounded model; kinematics,
- *   velocities and bias accelerations in FP32; the state, contact wrenches of
- *   contact mechanisms and a floating root's 6×6 solve in FP64.
+ *   bits, on the FP32 pipes) from the FP32-rounded model, and so do a
+ *   floating joint's 6×6 factor and solve; kinematics, velocities and bias
+ *   accelerations in FP32; the state in FP64.  A contact mechanism keeps its
+ *   world poses, body velocities, penetrations and contact-point velocities
+ *   (with their split into approach speed and tangential velocity) in FP64,
+ *   and runs the contact force law and wrench in FP32 from them.
  *   GPB_MIXED_REFINED always uses CRBA. */
 enum gpb_algorithm { GPB_ALGO_CRBA = 0, GPB_ALGO_ABA = 1 };
 
