@@ -41,6 +41,7 @@ int main() {
 
   // error-free transformations and the basic operations
   double e_sum = 0, e_add = 0, e_mul = 0, e_fma = 0, e_rcp = 0;
+  long add_order_differs = 0;
   for (int t = 0; t < 200000; ++t) {
     const double x = N(g) * std::exp(U(g)), y = N(g) * std::exp(U(g) * 0.2);
     const float a = (float)x, b = (float)y;
@@ -52,11 +53,16 @@ int main() {
       return (double)(std::fabs(got - ref) / (scale > 0 ? scale : 1));
     };
     e_add = std::fmax(e_add, rel(val(ff_add(X, Y)), xa + ya, std::fabs(xa) + std::fabs(ya)));
+    {  // commutative bit for bit (a reduction over lanes gives every lane the same sum)
+      const FF s1 = ff_add(X, Y), s2 = ff_add(Y, X);
+      add_order_differs += s1.hi != s2.hi || s1.lo != s2.lo;
+    }
     e_mul = std::fmax(e_mul, rel(val(ff_mul(X, Y)), xa * ya, std::fabs(xa * ya)));
     e_fma = std::fmax(e_fma, rel(val(ff_fma(X, Y, Z)), za + xa * ya, std::fabs(za) + std::fabs(xa * ya)));
     e_rcp = std::fmax(e_rcp, rel(val(ff_rcp(X)) * xa, 1.0L, 1.0L));
   }
   check("two_sum_abs_err", e_sum, 0.0);
+  check("ff_add_order_differs", (double)add_order_differs, 0.0);
   check("ff_add_rel_err", e_add, 3e-14);
   check("ff_mul_rel_err", e_mul, 3e-14);
   check("ff_fma_rel_err", e_fma, 3e-14);

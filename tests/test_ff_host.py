@@ -7,7 +7,8 @@ the round-to-nearest intrinsics they call (`__fadd_rn`, `__fmul_rn`,
 `__fmaf_rn`, ...; contraction off, so each is one correctly rounded FP32
 operation) and an `rsqrtf` perturbed by up to 2 ulp either way (the device one
 is approximate).  `tests/ff_host_check.cpp` checks them against long double:
-two_sum exact; ff_add, ff_mul, ff_fma, ff_rcp within 3e-14; ff_rsqrt within
+two_sum exact; ff_add commutative bit for bit; ff_add, ff_mul, ff_fma, ff_rcp
+within 3e-14; ff_rsqrt within
 3e-13 (one Newton step leaves 1.5·δ² of a start off by δ: 2.6e-14 from a
 correctly rounded FP32 start, 1.9e-13 from one 2 ulp off); the 6×6 factor of
 20,000 random spatial inertias (rigid bodies plus random articulated parts)
