@@ -8,12 +8,11 @@ the round-to-nearest intrinsics they call (`__fadd_rn`, `__fmul_rn`,
 operation) and an `rsqrtf` perturbed by up to 2 ulp either way (the device one
 is approximate).  `tests/ff_host_check.cpp` checks them against long double:
 two_sum exact; ff_add commutative bit for bit; ff_add, ff_mul, ff_fma, ff_rcp
-within 3e-14; ff_rsqrt within
-3e-13 (one Newton step leaves 1.5·δ² of a start off by δ: 2.6e-14 from a
-correctly rounded FP32 start, 1.9e-13 from one 2 ulp off); the 6×6 factor of
-20,000 random spatial inertias (rigid bodies plus random articulated parts)
-with its reciprocal pivots within 1e-12 and its solve within 1e-10 of max|x|;
-an indefinite matrix reported.
+within 3e-14; ff_rsqrt within 3e-13 (one Newton step leaves 1.5·δ² of a start
+off by δ: 2.6e-14 from a correctly rounded FP32 start, 1.9e-13 from one 2 ulp
+off); the 6×6 factor of 20,000 random spatial inertias (rigid bodies plus
+random articulated parts) with its reciprocal pivots within 1e-12 and its
+solve within 1e-10 of max|x|; an indefinite matrix reported.
 
 The contact law the mixed form runs in FP32 (`contact_force_parts` in
 `gpb_kernels.cu`, fed with the approach speed and tangential velocity formed in
