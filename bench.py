@@ -40,16 +40,22 @@ UNIT = "instance-steps/s"
 DT = {0: 1e-3, 1: 5e-4, 2: 1e-4, 3: 2e-4}
 CONFIG_NAME = {0: "acrobot", 1: "serial-chain", 2: "floating-cube", 3: "quadruped"}
 CONTROL = {0: "host", 1: "open_loop", 2: "host", 3: "pd"}
+# each configuration's own batch and length (1,024 acrobots × 10,000 steps;
+# 65,536 chains × 2,000; 32,768 cubes × 20,000; 16,384 quadrupeds × 10,000)
+CONFIG_INSTANCES = {0: 1024, 1: 65536, 2: 32768, 3: 16384}
+CONFIG_STEPS = {0: 10000, 1: 2000, 2: 20000, 3: 10000}
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: the configuration's own length; 2000 for --cuboids / --vstep)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpb", choices=["gpb", "reference"])
     ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--instances", type=int, default=65536)
+    ap.add_argument("--instances", type=int, default=None,
+                    help="instances per GPU (default: the configuration's own batch; 65536 for --cuboids / --vstep)")
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--mix-chains", type=int, default=0,
                     help="also step this many serial chains in the same batch (one control law for all)")
@@ -77,7 +83,13 @@ def parse():
     ap.add_argument("--pairs", type=int, default=1 << 22, help="collision queries per timed launch")
     ap.add_argument("--vstep", action="store_true",
                     help="velocity stepping (friction-cone impulses) on cubes resting on the ground")
-    return ap.parse_args()
+    args = ap.parse_args()
+    other = args.cuboids or args.vstep
+    if args.steps is None:
+        args.steps = 2000 if other else CONFIG_STEPS[args.config]
+    if args.instances is None:
+        args.instances = 65536 if other else CONFIG_INSTANCES[args.config]
+    return args
 
 
 def kernel_source_hash() -> str:
