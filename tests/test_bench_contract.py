@@ -33,6 +33,23 @@ def test_committed_headline_line():
             assert m["value"] <= d["value"] * (1 + 1e-12), name
 
 
+def test_configurations_default_to_their_own_batch_and_length(monkeypatch):
+    """`bench.py --config k` runs configuration k's own batch and length: 1,024
+    acrobots × 10,000 steps, 65,536 chains × 2,000 (the default run), 32,768
+    cubes × 20,000, 16,384 quadrupeds × 10,000, each at its own dt."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    want = {0: (1024, 10000, 1e-3), 1: (65536, 2000, 5e-4), 2: (32768, 20000, 1e-4), 3: (16384, 10000, 2e-4)}
+    for k, (n, steps, dt) in want.items():
+        monkeypatch.setattr(sys, "argv", ["bench.py", "--config", str(k)])
+        a = bench.parse()
+        assert (a.instances, a.steps, bench.DT[k]) == (n, steps, dt), k
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--gpus", "1", "--steps", "5", "--warmup", "3"])
+    a = bench.parse()
+    assert (a.config, a.instances, a.steps, a.warmup) == (1, 65536, 5, 3)
+
+
 def test_committed_lines_record_their_mapping():
     """Every committed bench line records each form's launch shape; where the
     autotuner chose several lanes per instance, the line carries the one-lane
